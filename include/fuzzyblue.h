@@ -1,0 +1,252 @@
+/*
+ * fuzzyblue.h — C ABI of the GB300 (sm_103a) atmosphere look-up-table precompute.
+ *
+ * This library replaces the Vulkan precompute path of the fuzzyblue crate
+ * (src/precompute.rs): the same parameters (km, 1/km), the same six passes
+ * (transmittance, direct irradiance, single scattering, scattering density,
+ * indirect irradiance, multiple scattering) and the same three output tables:
+ *
+ *   transmittance  2D  width = transmittance_mu_size, height = transmittance_r_size
+ *   irradiance     2D  width = irradiance_mu_s_size,  height = irradiance_r_size
+ *   scattering     3D  width = scattering_nu_size * scattering_mu_s_size,
+ *                      height = scattering_mu_size, depth = scattering_r_size
+ *
+ * Every table is RGBA, tightly packed, x fastest then y then z: the host layout
+ * that examples/dump.rs:150-194 obtains with vkCmdCopyImageToBuffer. Tables are
+ * RGBA32F in device memory (the scattering table can additionally be exported
+ * as RGBA16F, the format the reference allocates at src/precompute.rs:1215).
+ *
+ * Conventions: every entry point returns an int status (FB_OK = 0, negative on
+ * error) and never throws; handles are opaque; a handle may be used from one
+ * thread at a time; `stream` arguments are cudaStream_t passed as void*
+ * (NULL selects the builder's own stream). Work is enqueued asynchronously on
+ * the stream, the way Atmosphere::build records into a caller's command buffer.
+ */
+#ifndef FUZZYBLUE_H_
+#define FUZZYBLUE_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FB_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------- */
+#define FB_OK 0
+#define FB_NOT_READY 1            /* work still in flight (query/poll) */
+#define FB_ERR_INVALID_ARGUMENT (-1)
+#define FB_ERR_INVALID_PARAMS (-2) /* rejected by fb_params_validate */
+#define FB_ERR_OUT_OF_MEMORY (-3)
+#define FB_ERR_CUDA (-4)
+#define FB_ERR_BUDGET (-5)         /* request larger than the serving HBM budget */
+#define FB_ERR_CANCELLED (-6)
+#define FB_ERR_NOT_FOUND (-7)
+#define FB_ERR_SHUTDOWN (-8)
+#define FB_ERR_NO_KERNEL (-9)      /* no sm_103a image for the current device */
+
+/* ---- parameters ----------------------------------------------------------- */
+
+/* One layer of a density profile: clamp(exp_term*exp(exp_scale*h) +
+ * linear_term*h + constant_term, 0, 1). Replaces DensityProfileLayer
+ * (src/precompute.rs:660-666); padded to the 32-byte std140 array stride of
+ * DensityProfileLayerRaw (src/precompute.rs:1012-1021). */
+typedef struct fb_density_profile_layer {
+    float width;
+    float exp_term;
+    float exp_scale;
+    float linear_term;
+    float constant_term;
+    float _pad[3];
+} fb_density_profile_layer;
+
+/* Two layers, bottom to top; the width of the last one is ignored.
+ * Replaces DensityProfile (src/precompute.rs:674-676). */
+typedef struct fb_density_profile {
+    fb_density_profile_layer layers[2];
+} fb_density_profile;
+
+/* Byte-for-byte the 320-byte ParamsRaw uniform block
+ * (src/precompute.rs:937-964 == shaders/params.h:26-87 in std140). */
+typedef struct fb_params_raw {
+    float solar_irradiance[3];
+    float sun_angular_radius;
+    float rayleigh_scattering[3];
+    float bottom_radius;
+    float mie_scattering[3];
+    float top_radius;
+    float mie_extinction[3];
+    float mie_phase_function_g;
+    float ground_albedo[3];
+    float mu_s_min;
+    float absorption_extinction[3];
+    uint32_t transmittance_mu_size;
+    uint32_t transmittance_r_size;
+    uint32_t scattering_r_size;
+    uint32_t scattering_mu_size;
+    uint32_t scattering_mu_s_size;
+    uint32_t scattering_nu_size;
+    uint32_t irradiance_mu_s_size;
+    uint32_t irradiance_r_size;
+    uint32_t _pad0;
+    fb_density_profile rayleigh_density;
+    fb_density_profile mie_density;
+    fb_density_profile absorption_density;
+} fb_params_raw;
+
+/* Arithmetic of the passes. PLAIN is one FP32 atmosphere exactly as the
+ * reference's shaders compute it. MIXED keeps FP32 bulk work but uses
+ * compensated (Kahan) quadrature sums and FP64 for the ray/sphere
+ * discriminants, the texture-coordinate mappings at the horizon seam and the
+ * accumulation of orders into the final tables. */
+#define FB_PRECISION_PLAIN 0u
+#define FB_PRECISION_MIXED 1u
+
+/* Storage of the five scattering-class tables. F32 keeps every table RGBA32F.
+ * F16 rounds every scattering-class texel to half precision when it is
+ * stored, as the reference's RGBA16F images do (src/precompute.rs:1215). */
+#define FB_STORAGE_F32 0u
+#define FB_STORAGE_F16 1u
+
+/* Parameters of one atmosphere: the ParamsRaw block plus the fields the
+ * reference keeps elsewhere (Parameters::order, src/precompute.rs:700) or as
+ * shader constants (sample counts). Vulkan-only fields of Parameters (usage,
+ * stage/access masks, layout) have no counterpart. 384 bytes. */
+typedef struct fb_params {
+    fb_params_raw raw;
+    uint32_t order;                     /* number of bounces, >= 1 (default 4) */
+    uint32_t transmittance_steps;       /* transmittance.comp:14, default 500 */
+    uint32_t single_scattering_steps;   /* single_scattering.comp:42, default 50 */
+    uint32_t multiple_scattering_steps; /* multiple_scattering.comp:21, default 50 */
+    uint32_t density_samples;           /* scattering_density.comp:34, default 16
+                                           (16 theta x 32 phi directions) */
+    uint32_t irradiance_samples;        /* indirect_irradiance.comp:20, default 32
+                                           (16 theta x 64 phi directions) */
+    uint32_t precision;                 /* FB_PRECISION_* */
+    uint32_t storage;                   /* FB_STORAGE_* */
+    uint32_t reserved[8];
+} fb_params;
+
+typedef struct fb_extent {
+    uint32_t width;
+    uint32_t height;
+    uint32_t depth;
+} fb_extent;
+
+/* Parameters::default() (src/precompute.rs:849-935) plus the default
+ * extension fields. */
+void fb_params_default(fb_params* out);
+
+/* Checks sizes and geometry; FB_OK or FB_ERR_INVALID_PARAMS. Sizes must be
+ * >= 2, scattering_mu_size even, top_radius > bottom_radius > 0, order >= 1,
+ * sample counts within [1, 4096] (density/irradiance samples even, <= 64). */
+int fb_params_validate(const fb_params* p);
+
+/* Parameters::{transmittance,irradiance,scattering}_extent
+ * (src/precompute.rs:771-793). Any pointer may be NULL. */
+int fb_params_extents(const fb_params* p, fb_extent* transmittance,
+                      fb_extent* irradiance, fb_extent* scattering);
+
+/* Device bytes one build needs: the three outputs plus the temporaries. */
+int fb_params_device_bytes(const fb_params* p, uint64_t* output_bytes,
+                           uint64_t* temporary_bytes);
+
+/* ---- builder ------------------------------------------------------------- */
+
+typedef struct fb_builder fb_builder;
+typedef struct fb_atmosphere fb_atmosphere;
+typedef struct fb_pending fb_pending;
+
+/* Replaces Builder::new (src/precompute.rs:61-68): binds a CUDA device, creates
+ * the builder's stream and checks that the sm_103a kernels load. */
+int fb_builder_create(int device, fb_builder** out);
+void fb_builder_destroy(fb_builder* b);
+int fb_builder_device(const fb_builder* b, int* device);
+/* Number of SMs, used to size persistent launches. */
+int fb_builder_sm_count(const fb_builder* b, int* sms);
+
+/* Host-side allocation hook: when set, every device allocation the builder
+ * makes goes through `alloc` (return NULL to report failure) and `release`.
+ * Used to inject allocation failures in tests; NULL restores cudaMallocAsync. */
+typedef void* (*fb_alloc_fn)(void* user, size_t bytes, void* stream);
+typedef void (*fb_free_fn)(void* user, void* ptr, void* stream);
+int fb_builder_set_allocator(fb_builder* b, fb_alloc_fn alloc, fb_free_fn release,
+                             void* user);
+
+/* ---- one atmosphere ------------------------------------------------------ */
+
+/* Replaces Atmosphere::build (src/precompute.rs:1077-2073): allocates the
+ * outputs and temporaries and enqueues every pass on `stream`. Returns at once;
+ * the tables are ready when the pending handle reports FB_OK. */
+int fb_atmosphere_build(fb_builder* b, void* stream, const fb_params* p,
+                        fb_pending** out);
+
+/* FB_OK when all work of the build has completed, FB_NOT_READY otherwise. */
+int fb_pending_query(fb_pending* p);
+/* Blocks until the build completed (PendingAtmosphere::assert_ready,
+ * src/precompute.rs:2209, after the caller's wait). */
+int fb_pending_wait(fb_pending* p);
+/* Makes `consumer_stream` wait for the build (an event wait): the stream
+ * analogue of PendingAtmosphere::acquire_ownership (src/precompute.rs:2147). */
+int fb_pending_acquire(fb_pending* p, void* consumer_stream);
+/* Number of atmospheres the pending handle carries (1, or the batch size). */
+int fb_pending_count(const fb_pending* p, uint32_t* count);
+/* PendingAtmosphere::atmosphere (src/precompute.rs:2204): borrows atmosphere
+ * `index`; it stays owned by the pending handle until fb_pending_take. */
+int fb_pending_atmosphere(fb_pending* p, uint32_t index, fb_atmosphere** out);
+/* Transfers ownership of atmosphere `index` to the caller (who then calls
+ * fb_atmosphere_destroy). Waits for completion first. */
+int fb_pending_take(fb_pending* p, uint32_t index, fb_atmosphere** out);
+/* Drop for PendingAtmosphere (src/precompute.rs:2122-2140): frees the
+ * temporaries (stream-ordered) and every atmosphere not taken. */
+void fb_pending_release(fb_pending* p);
+
+typedef struct fb_tables {
+    void* transmittance; /* float4, transmittance extent */
+    void* irradiance;    /* float4, irradiance extent */
+    void* scattering;    /* float4, scattering extent */
+    fb_extent transmittance_extent;
+    fb_extent irradiance_extent;
+    fb_extent scattering_extent;
+} fb_tables;
+
+/* Device pointers and extents: the accessors of src/precompute.rs:2075-2101. */
+int fb_atmosphere_tables(const fb_atmosphere* a, fb_tables* out);
+/* Enqueues device->host copies of the three tables (any pointer may be NULL)
+ * on `stream` and waits for them. Host buffers hold width*height*depth*4
+ * floats each. */
+int fb_atmosphere_copy_to_host(const fb_atmosphere* a, void* stream,
+                               float* transmittance, float* irradiance,
+                               float* scattering);
+/* RGBA16F copy of the scattering table (the reference's image format,
+ * src/precompute.rs:1215; examples/dump.rs:120): `out` holds
+ * width*height*depth*4 uint16 half floats, round to nearest even. */
+int fb_atmosphere_export_scattering_f16(const fb_atmosphere* a, void* stream,
+                                        uint16_t* out);
+int fb_atmosphere_params(const fb_atmosphere* a, fb_params* out);
+/* Drop for Atmosphere (src/precompute.rs:1059-1075). */
+void fb_atmosphere_destroy(fb_atmosphere* a);
+
+/* ---- batches ------------------------------------------------------------- */
+
+/* Builds `count` atmospheres with one persistent launch per pass group,
+ * whatever their table sizes, orders and precision; the order iteration is
+ * replayed from a CUDA graph. Atmospheres are read with
+ * fb_pending_atmosphere(p, i, ...). */
+int fb_batch_build(fb_builder* b, void* stream, const fb_params* params,
+                   uint32_t count, fb_pending** out);
+
+/* ---- diagnostics --------------------------------------------------------- */
+
+const char* fb_status_string(int status);
+/* Message of the last error on the calling thread ("" if none). */
+const char* fb_last_error(void);
+int fb_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FUZZYBLUE_H_ */
