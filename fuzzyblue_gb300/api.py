@@ -1,0 +1,289 @@
+"""Python mirror of the crate's public API (src/lib.rs:9: Atmosphere, Builder,
+Parameters, PendingAtmosphere), over the C ABI of include/fuzzyblue.h.
+
+    builder = Builder(device=0)                      # Builder::new
+    pending = Atmosphere.build(builder, Parameters()) # Atmosphere::build
+    pending.wait(); pending.assert_ready()            # device_wait_idle + assert_ready
+    atm = pending.atmosphere()                       # PendingAtmosphere::atmosphere
+    atm.transmittance(), atm.scattering_extent() ...  # accessors, src/precompute.rs:2075-2101
+
+Streams: any argument named `stream` accepts None (the builder's stream), a
+torch.cuda.Stream, or a raw cudaStream_t as an int.
+"""
+from __future__ import annotations
+
+import ctypes
+from typing import Dict, List, Optional, Sequence
+
+import numpy as np
+
+from . import _native as N
+from .params import Parameters, c_params
+
+
+def _stream_handle(stream) -> Optional[int]:
+    if stream is None:
+        return None
+    if isinstance(stream, int):
+        return stream
+    h = getattr(stream, "cuda_stream", None)
+    if h is not None:
+        return int(h)
+    raise TypeError("unsupported stream object %r" % (stream,))
+
+
+class DeviceArray:
+    """A view of device memory exposing __cuda_array_interface__ (float32),
+    so torch.as_tensor(view, device='cuda') wraps it without a copy."""
+
+    def __init__(self, ptr: int, shape, owner=None, typestr="<f4"):
+        self.ptr = int(ptr)
+        self.shape = tuple(int(s) for s in shape)
+        self._owner = owner
+        self.__cuda_array_interface__ = {"shape": self.shape, "typestr": typestr, "data": (self.ptr, False),
+                                         "version": 3, "strides": None}
+
+    def to_numpy(self) -> np.ndarray:
+        import torch
+        t = torch.as_tensor(self, device="cuda")
+        return t.cpu().numpy()
+
+
+class Builder:
+    """Builder::new (src/precompute.rs:61-68): one CUDA device and its kernels."""
+
+    def __init__(self, device: int = 0):
+        self._h = ctypes.c_void_p()
+        N.check(N.lib().fb_builder_create(device, ctypes.byref(self._h)), "fb_builder_create")
+        self._alloc_refs = None
+
+    @property
+    def handle(self):
+        return self._h
+
+    @property
+    def sm_count(self) -> int:
+        v = ctypes.c_int()
+        N.check(N.lib().fb_builder_sm_count(self._h, ctypes.byref(v)), "fb_builder_sm_count")
+        return v.value
+
+    def set_profiling(self, enabled: bool = True):
+        N.check(N.lib().fb_builder_set_profiling(self._h, 1 if enabled else 0), "fb_builder_set_profiling")
+
+    def set_allocator(self, alloc, release):
+        """Routes the builder's device allocations through Python callables
+        alloc(nbytes, stream) -> int pointer (0 = failure) and release(ptr, stream)."""
+        if alloc is None:
+            N.check(N.lib().fb_builder_set_allocator(self._h, N.ALLOC_FN(), N.FREE_FN(), None), "set_allocator")
+            self._alloc_refs = None
+            return
+        a = N.ALLOC_FN(lambda user, n, s: alloc(n, s) or None)
+        f = N.FREE_FN(lambda user, p, s: release(p, s))
+        N.check(N.lib().fb_builder_set_allocator(self._h, a, f, None), "set_allocator")
+        self._alloc_refs = (a, f)
+
+    def close(self):
+        if self._h:
+            N.lib().fb_builder_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Atmosphere:
+    """An atmosphere whose tables are ready (src/precompute.rs:1042-1101)."""
+
+    def __init__(self, handle, params: Parameters, owned: bool, keepalive=None):
+        self._h = handle
+        self.params = params
+        self._owned = owned
+        self._keep = keepalive
+
+    # -- Atmosphere::build ---------------------------------------------------
+    @staticmethod
+    def build(builder: Builder, params: Parameters, stream=None) -> "PendingAtmosphere":
+        c = params.to_c()
+        out = ctypes.c_void_p()
+        N.check(N.lib().fb_atmosphere_build(builder.handle, _stream_handle(stream), ctypes.byref(c),
+                                            ctypes.byref(out)), "fb_atmosphere_build")
+        return PendingAtmosphere(out, [params], builder)
+
+    # -- accessors (src/precompute.rs:2075-2101) ------------------------------
+    def _tables(self) -> N.c_tables:
+        t = N.c_tables()
+        N.check(N.lib().fb_atmosphere_tables(self._h, ctypes.byref(t)), "fb_atmosphere_tables")
+        return t
+
+    def transmittance(self) -> int:
+        return self._tables().transmittance
+
+    def irradiance(self) -> int:
+        return self._tables().irradiance
+
+    def scattering(self) -> int:
+        return self._tables().scattering
+
+    def transmittance_extent(self):
+        return self.params.transmittance_extent()
+
+    def irradiance_extent(self):
+        return self.params.irradiance_extent()
+
+    def scattering_extent(self):
+        return self.params.scattering_extent()
+
+    def device_views(self) -> Dict[str, DeviceArray]:
+        t = self._tables()
+        tw, th = self.params.transmittance_extent()
+        iw, ih = self.params.irradiance_extent()
+        sw, sh, sd = self.params.scattering_extent()
+        return {
+            "transmittance": DeviceArray(t.transmittance, (th, tw, 4), self),
+            "irradiance": DeviceArray(t.irradiance, (ih, iw, 4), self),
+            "scattering": DeviceArray(t.scattering, (sd, sh, sw, 4), self),
+        }
+
+    def to_host(self, stream=None) -> Dict[str, np.ndarray]:
+        """Copies the three tables to host memory: RGBA float32 arrays shaped
+        (height, width, 4) and (depth, height, width, 4)."""
+        tw, th = self.params.transmittance_extent()
+        iw, ih = self.params.irradiance_extent()
+        sw, sh, sd = self.params.scattering_extent()
+        out = {
+            "transmittance": np.empty((th, tw, 4), np.float32),
+            "irradiance": np.empty((ih, iw, 4), np.float32),
+            "scattering": np.empty((sd, sh, sw, 4), np.float32),
+        }
+        N.check(N.lib().fb_atmosphere_copy_to_host(self._h, _stream_handle(stream),
+                                                   out["transmittance"].ctypes.data, out["irradiance"].ctypes.data,
+                                                   out["scattering"].ctypes.data), "fb_atmosphere_copy_to_host")
+        return out
+
+    def export_scattering_f16(self, stream=None) -> np.ndarray:
+        """The scattering table as RGBA16F (np.float16), the reference's image format."""
+        sw, sh, sd = self.params.scattering_extent()
+        out = np.empty((sd, sh, sw, 4), np.float16)
+        N.check(N.lib().fb_atmosphere_export_scattering_f16(self._h, _stream_handle(stream), out.ctypes.data),
+                "fb_atmosphere_export_scattering_f16")
+        return out
+
+    def close(self):
+        if self._owned and self._h:
+            N.lib().fb_atmosphere_destroy(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class PendingAtmosphere:
+    """An atmosphere (or batch) being prepared by the GPU (src/precompute.rs:2103-2212)."""
+
+    def __init__(self, handle, params: Sequence[Parameters], builder: Builder):
+        self._h = handle
+        self.params = list(params)
+        self._builder = builder  # keeps the builder alive
+        self._taken = set()
+
+    def __len__(self):
+        n = ctypes.c_uint32()
+        N.check(N.lib().fb_pending_count(self._h, ctypes.byref(n)), "fb_pending_count")
+        return n.value
+
+    def query(self) -> bool:
+        return N.check(N.lib().fb_pending_query(self._h), "fb_pending_query") == N.FB_OK
+
+    def wait(self):
+        N.check(N.lib().fb_pending_wait(self._h), "fb_pending_wait")
+
+    def assert_ready(self):
+        """PendingAtmosphere::assert_ready (src/precompute.rs:2209): the work
+        must have completed."""
+        if not self.query():
+            raise RuntimeError("atmosphere build has not completed")
+
+    def acquire(self, stream):
+        """Makes `stream` wait for the build (acquire_ownership, src/precompute.rs:2147)."""
+        N.check(N.lib().fb_pending_acquire(self._h, _stream_handle(stream)), "fb_pending_acquire")
+
+    def atmosphere(self, index: int = 0) -> Atmosphere:
+        h = ctypes.c_void_p()
+        N.check(N.lib().fb_pending_atmosphere(self._h, index, ctypes.byref(h)), "fb_pending_atmosphere")
+        return Atmosphere(h, self.params[index], owned=False, keepalive=self)
+
+    def take(self, index: int = 0) -> Atmosphere:
+        h = ctypes.c_void_p()
+        N.check(N.lib().fb_pending_take(self._h, index, ctypes.byref(h)), "fb_pending_take")
+        return Atmosphere(h, self.params[index], owned=True)
+
+    def intermediates(self, index: int = 0) -> Dict[str, DeviceArray]:
+        m = N.c_intermediates()
+        N.check(N.lib().fb_pending_intermediates(self._h, index, ctypes.byref(m)), "fb_pending_intermediates")
+        p = self.params[index]
+        iw, ih = p.irradiance_extent()
+        sw, sh, sd = p.scattering_extent()
+        sc = (sd, sh, sw, 4)
+        return {
+            "delta_irradiance_0": DeviceArray(m.delta_irradiance[0], (ih, iw, 4), self),
+            "delta_irradiance_1": DeviceArray(m.delta_irradiance[1], (ih, iw, 4), self),
+            "delta_rayleigh": DeviceArray(m.delta_rayleigh, sc, self),
+            "delta_mie": DeviceArray(m.delta_mie, sc, self),
+            "delta_multiple_scattering": DeviceArray(m.delta_multiple_scattering, sc, self),
+            "scattering_density": DeviceArray(m.scattering_density, sc, self),
+        }
+
+    def profile(self) -> List[dict]:
+        """Per-launch device times of the build (profiling must have been on)."""
+        n = ctypes.c_uint32()
+        N.check(N.lib().fb_pending_profile(self._h, None, 0, ctypes.byref(n)), "fb_pending_profile")
+        arr = (N.c_launch_profile * max(n.value, 1))()
+        N.check(N.lib().fb_pending_profile(self._h, arr, n.value, ctypes.byref(n)), "fb_pending_profile")
+        return [{"kernel": N.KERNEL_NAMES[r.kernel], "order": r.order, "precision": r.precision, "grid": r.grid,
+                 "items": r.items, "texels": r.texels, "ms": r.ms} for r in arr[:n.value]]
+
+    def release(self):
+        if self._h:
+            N.lib().fb_pending_release(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.release()
+        except Exception:
+            pass
+
+
+def build_batch(builder: Builder, params: Sequence[Parameters], stream=None) -> PendingAtmosphere:
+    """Builds many atmospheres (any mix of table sizes, orders and precision
+    modes) with one persistent launch per pass group, replayed from a CUDA graph."""
+    arr = (c_params * len(params))(*[p.to_c() for p in params])
+    out = ctypes.c_void_p()
+    N.check(N.lib().fb_batch_build(builder.handle, _stream_handle(stream), arr, len(params), ctypes.byref(out)),
+            "fb_batch_build")
+    return PendingAtmosphere(out, params, builder)
+
+
+def validate(params: Parameters) -> None:
+    c = params.to_c()
+    N.check(N.lib().fb_params_validate(ctypes.byref(c)), "fb_params_validate")
+
+
+def device_bytes(params: Parameters):
+    c = params.to_c()
+    o = ctypes.c_uint64()
+    t = ctypes.c_uint64()
+    N.check(N.lib().fb_params_device_bytes(ctypes.byref(c), ctypes.byref(o), ctypes.byref(t)), "device_bytes")
+    return o.value, t.value

@@ -1,0 +1,500 @@
+// fb_device.cuh — device-side data of one atmosphere and the shared math of
+// the six precompute passes (sm_103a).
+//
+// Two arithmetic modes are compiled from the same templates:
+//   PLAIN (MX = false): FP32, operation for operation the arithmetic of the
+//     reference's shaders (shaders/*.h, *.comp). The translation unit that
+//     instantiates it is compiled with --fmad=false, so products and sums round
+//     separately as in the shaders; fmaf() is used only in interpolation and
+//     accumulation, where it changes nothing but the last bit.
+//   MIXED (MX = true): a point on a ray is carried as (q, s) = (r^2 - R^2, r*mu)
+//     in FP64, which removes the cancellations at the horizon (ground altitude,
+//     ray/sphere discriminants, the horizon seam of the mu coordinate); quadrature
+//     sums are Kahan-compensated; orders accumulate in FP64.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+namespace fb {
+
+struct Layer {
+  float width, exp_term, exp_scale, linear_term, constant_term;
+};
+
+// One atmosphere as the kernels see it: parameters (ParamsRaw fields,
+// src/precompute.rs:937-964), sizes, sample counts and its tables.
+struct DevAtmo {
+  float solar[3], rayleigh[3], mie_sca[3], mie_ext[3], albedo[3], absorption[3];
+  float sun_radius, bottom, top, g, mu_s_min;
+  Layer ray_d[2], mie_d[2], abs_d[2];
+  int tr_mu, tr_r, sc_r, sc_mu, sc_mus, sc_nu, ir_mus, ir_r;
+  int tr_steps, ss_steps, ms_steps, dens_n, irr_n, order;
+  int f16;         // round the scattering-class tables to half on store
+  int W;           // sc_nu * sc_mus, width of the packed 3D scattering tables
+  int dens_chunk;  // mu rows per scattering-density tile (autotuned per table class)
+  // outputs
+  float4* tr;
+  float4* ir;
+  float4* sc;
+  // temporaries
+  float4* dirr[2];  // delta irradiance, ping-pong by order parity
+  float4* dr;       // delta Rayleigh (single)
+  float4* dm;       // delta Mie (single)
+  float4* dms;      // delta multiple scattering of the last order
+  float4* dens;     // scattering density of the current order
+  double* sc_acc;   // MIXED: FP64 running sum of scattering rgb (3 per texel)
+  double* ir_acc;   // MIXED: FP64 running sum of irradiance rgb (3 per texel)
+};
+
+constexpr float kPiF = 3.14159265358979323846f;
+constexpr double kPiD = 3.14159265358979323846;
+
+// --------------------------------------------------------------- GLSL basics
+__device__ __forceinline__ float gmin(float x, float y) { return y < x ? y : x; }
+__device__ __forceinline__ float gmax(float x, float y) { return x < y ? y : x; }
+__device__ __forceinline__ float gclamp(float x, float lo, float hi) { return gmin(gmax(x, lo), hi); }
+__device__ __forceinline__ double gmin(double x, double y) { return y < x ? y : x; }
+__device__ __forceinline__ double gmax(double x, double y) { return x < y ? y : x; }
+__device__ __forceinline__ double gclamp(double x, double lo, double hi) { return gmin(gmax(x, lo), hi); }
+
+template <class T> __device__ __forceinline__ T clamp_cosine(T mu) { return gclamp(mu, T(-1), T(1)); }
+__device__ __forceinline__ float safe_sqrt(float a) { return sqrtf(gmax(a, 0.0f)); }
+__device__ __forceinline__ double safe_sqrt(double a) { return sqrt(gmax(a, 0.0)); }
+
+// util.h:18-24
+template <class T> __device__ __forceinline__ T coord_from_unit(T x, int n) {
+  return T(0.5) / T(n) + x * (T(1) - T(1) / T(n));
+}
+template <class T> __device__ __forceinline__ T unit_from_coord(T u, int n) {
+  return (u - T(0.5) / T(n)) / (T(1) - T(1) / T(n));
+}
+// util.h:26-34
+__device__ __forceinline__ float phase_rayleigh(float nu) {
+  const float k = 3.0f / (16.0f * kPiF);
+  return k * (1.0f + nu * nu);
+}
+__device__ __forceinline__ float phase_mie(float g, float nu) {
+  const float k = 3.0f / (8.0f * kPiF) * (1.0f - g * g) / (2.0f + g * g);
+  return k * (1.0f + nu * nu) / powf(1.0f + g * g - 2.0f * g * nu, 1.5f);
+}
+// util.h:36-38
+__device__ __forceinline__ float frag_from_texel(uint32_t i, uint32_t n) {
+  return float(n) * coord_from_unit(float(i) / float(n - 1), int(n));
+}
+__device__ __forceinline__ double frag_from_texel_d(uint32_t i, uint32_t n) {
+  return double(n) * coord_from_unit(double(i) / double(n - 1), int(n));
+}
+__device__ __forceinline__ float smoothstepf(float e0, float e1, float x) {
+  float t = gclamp((x - e0) / (e1 - e0), 0.0f, 1.0f);
+  return t * t * (3.0f - 2.0f * t);
+}
+
+// params.h:89-99 — density profiles.
+__device__ __forceinline__ float layer_density(const Layer& L, float h) {
+  float d = L.exp_term * expf(L.exp_scale * h) + L.linear_term * h + L.constant_term;
+  return gclamp(d, 0.0f, 1.0f);
+}
+__device__ __forceinline__ float profile_density(const Layer* P, float h) {
+  return h < P[0].width ? layer_density(P[0], h) : layer_density(P[1], h);
+}
+
+// ------------------------------------------------------------ table access
+// One axis of the LINEAR + CLAMP_TO_EDGE sampler of src/precompute.rs:85-98:
+// texel coordinate u*n - 0.5, neighbours clamped to [0, n-1].
+struct Axis {
+  int i0, i1;
+  float f;
+};
+__device__ __forceinline__ Axis make_axis(float coord, int n) {
+  float x = coord * float(n) - 0.5f;
+  float fl = floorf(x);
+  Axis a;
+  a.f = x - fl;
+  fl = fminf(fmaxf(fl, -1.0f), float(n));  // fmaxf(NaN, -1) = -1
+  int i = (int)fl;
+  a.i0 = min(max(i, 0), n - 1);
+  a.i1 = min(max(i + 1, 0), n - 1);
+  return a;
+}
+
+__device__ __forceinline__ float4 ld4(const float4* p) { return __ldg(p); }
+__device__ __forceinline__ float3 f3(float4 v) { return make_float3(v.x, v.y, v.z); }
+
+// Bilinear RGB fetch with the Vulkan weight order (1-a)(1-b), a(1-b), (1-a)b, ab.
+__device__ __forceinline__ float3 fetch2(const float4* t, int w, Axis x, Axis y) {
+  const float4 p00 = ld4(t + y.i0 * w + x.i0), p10 = ld4(t + y.i0 * w + x.i1);
+  const float4 p01 = ld4(t + y.i1 * w + x.i0), p11 = ld4(t + y.i1 * w + x.i1);
+  const float w00 = (1.0f - x.f) * (1.0f - y.f), w10 = x.f * (1.0f - y.f);
+  const float w01 = (1.0f - x.f) * y.f, w11 = x.f * y.f;
+  float3 o;
+  o.x = fmaf(w11, p11.x, fmaf(w01, p01.x, fmaf(w10, p10.x, w00 * p00.x)));
+  o.y = fmaf(w11, p11.y, fmaf(w01, p01.y, fmaf(w10, p10.y, w00 * p00.y)));
+  o.z = fmaf(w11, p11.z, fmaf(w01, p01.z, fmaf(w10, p10.z, w00 * p00.z)));
+  return o;
+}
+
+// Trilinear RGB fetch from a packed 3D table (width w, height h), same weights.
+__device__ __forceinline__ float3 fetch3(const float4* t, int w, int h, Axis x, Axis y, Axis z) {
+  const float ia = 1.0f - x.f, ib = 1.0f - y.f, ic = 1.0f - z.f;
+  const float wt[8] = {ia * ib * ic, x.f * ib * ic, ia * y.f * ic, x.f * y.f * ic,
+                       ia * ib * z.f, x.f * ib * z.f, ia * y.f * z.f, x.f * y.f * z.f};
+  const int xs[2] = {x.i0, x.i1}, ys[2] = {y.i0, y.i1}, zs[2] = {z.i0, z.i1};
+  float3 o = make_float3(0.f, 0.f, 0.f);
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const float4 p = ld4(t + ((size_t)zs[k >> 2] * h + ys[(k >> 1) & 1]) * w + xs[k & 1]);
+    o.x = fmaf(wt[k], p.x, o.x);
+    o.y = fmaf(wt[k], p.y, o.y);
+    o.z = fmaf(wt[k], p.z, o.z);
+  }
+  return o;
+}
+
+__device__ __forceinline__ float3 operator+(float3 a, float3 b) { return make_float3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ float3 operator*(float3 a, float3 b) { return make_float3(a.x * b.x, a.y * b.y, a.z * b.z); }
+__device__ __forceinline__ float3 operator/(float3 a, float3 b) { return make_float3(a.x / b.x, a.y / b.y, a.z / b.z); }
+__device__ __forceinline__ float3 operator*(float3 a, float s) { return make_float3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float3 ld3(const float* v) { return make_float3(v[0], v[1], v[2]); }
+__device__ __forceinline__ float3 min1(float3 q) { return make_float3(gmin(q.x, 1.f), gmin(q.y, 1.f), gmin(q.z, 1.f)); }
+
+// Kahan-compensated accumulator of an RGB sum.
+struct Kahan3 {
+  float3 s, c;
+  __device__ __forceinline__ void init() {
+    s = make_float3(0.f, 0.f, 0.f);
+    c = s;
+  }
+  __device__ __forceinline__ static void add1(float& sum, float& comp, float v) {
+    float y = v - comp;
+    float t = sum + y;
+    comp = (t - sum) - y;
+    sum = t;
+  }
+  __device__ __forceinline__ void add(float3 v) {
+    add1(s.x, c.x, v.x);
+    add1(s.y, c.y, v.y);
+    add1(s.z, c.z, v.z);
+  }
+};
+
+__device__ __forceinline__ float store_round(float v, int f16) {
+  return f16 ? __half2float(__float2half_rn(v)) : v;
+}
+__device__ __forceinline__ float4 store_round4(float4 v, int f16) {
+  if (!f16) return v;
+  return make_float4(store_round(v.x, 1), store_round(v.y, 1), store_round(v.z, 1), store_round(v.w, 1));
+}
+
+// ------------------------------------------------------ PLAIN (FP32) geometry
+// The reference's formulas, term by term.
+struct Geo32 {
+  float R, T, H;  // bottom, top, sqrt(T^2 - R^2)
+  __device__ __forceinline__ void init(const DevAtmo& a) {
+    R = a.bottom;
+    T = a.top;
+    H = sqrtf(T * T - R * R);
+  }
+  // params.h:105-124
+  __device__ __forceinline__ float dist_top(float r, float mu) const {
+    float disc = r * r * (mu * mu - 1.0f) + T * T;
+    return gmax(-r * mu + safe_sqrt(disc), 0.0f);
+  }
+  __device__ __forceinline__ float dist_bottom(float r, float mu) const {
+    float disc = r * r * (mu * mu - 1.0f) + R * R;
+    return gmax(-r * mu - safe_sqrt(disc), 0.0f);
+  }
+  __device__ __forceinline__ bool hits_ground(float r, float mu) const {
+    return mu < 0.0f && r * r * (mu * mu - 1.0f) + R * R >= 0.0f;
+  }
+  __device__ __forceinline__ float clamp_radius(float r) const { return gclamp(r, R, T); }
+  // transmittance.h:7-24
+  __device__ __forceinline__ void tr_coords(const DevAtmo& a, float r, float mu, float& u, float& v) const {
+    float rho = safe_sqrt(r * r - R * R);
+    float d = dist_top(r, mu);
+    float d_min = T - r;
+    float d_max = rho + H;
+    float x_mu = (d - d_min) / (d_max - d_min);
+    float x_r = rho / H;
+    u = coord_from_unit(x_mu, a.tr_mu);
+    v = coord_from_unit(x_r, a.tr_r);
+  }
+  // transmittance.h:26-33
+  __device__ __forceinline__ float3 tr_to_top(const DevAtmo& a, float r, float mu) const {
+    float u, v;
+    tr_coords(a, r, mu, u, v);
+    return fetch2(a.tr, a.tr_mu, make_axis(u, a.tr_mu), make_axis(v, a.tr_r));
+  }
+  // transmittance.h:35-61
+  __device__ __forceinline__ float3 tr_segment(const DevAtmo& a, float r, float mu, float d, bool ground) const {
+    float r_d = clamp_radius(sqrtf(d * d + 2.0f * r * mu * d + r * r));
+    float mu_d = clamp_cosine((r * mu + d) / r_d);
+    float3 q = ground ? tr_to_top(a, r_d, -mu_d) / tr_to_top(a, r, -mu)
+                      : tr_to_top(a, r, mu) / tr_to_top(a, r_d, mu_d);
+    return min1(q);
+  }
+  // scattering.h:15-46 — the r and mu texture coordinates (w and z).
+  __device__ __forceinline__ float u_r(const DevAtmo& a, float r) const {
+    float rho = safe_sqrt(r * r - R * R);
+    return coord_from_unit(rho / H, a.sc_r);
+  }
+  __device__ __forceinline__ float u_mu(const DevAtmo& a, float r, float mu, bool ground) const {
+    float rho = safe_sqrt(r * r - R * R);
+    float r_mu = r * mu;
+    float disc = r_mu * r_mu - r * r + R * R;
+    if (ground) {
+      float d = -r_mu - safe_sqrt(disc);
+      float d_min = r - R;
+      float d_max = rho;
+      return 0.5f - 0.5f * coord_from_unit(d_max == d_min ? 0.0f : (d - d_min) / (d_max - d_min), a.sc_mu / 2);
+    }
+    float d = -r_mu + safe_sqrt(disc + H * H);
+    float d_min = T - r;
+    float d_max = rho + H;
+    return 0.5f + 0.5f * coord_from_unit((d - d_min) / (d_max - d_min), a.sc_mu / 2);
+  }
+  // scattering.h:48-56 — the mu_s texture coordinate.
+  __device__ __forceinline__ float u_mu_s(const DevAtmo& a, float mu_s) const {
+    float d = dist_top(R, mu_s);
+    float d_min = T - R;
+    float d_max = H;
+    float aa = (d - d_min) / (d_max - d_min);
+    float A = -2.0f * a.mu_s_min * R / (d_max - d_min);
+    return coord_from_unit(gmax(1.0f - aa / A, 0.0f) / (1.0f + aa), a.sc_mus);
+  }
+};
+
+// ------------------------------------------------------ MIXED (FP64) geometry
+// A point on a ray is (q, s) = (r^2 - R^2, r*mu). Moving a distance d along the
+// ray gives q' = q + d (2 s + d) and s' = s + d exactly, so the altitude
+// h = q / (r + R), the horizon distance rho = sqrt(q) and the ground
+// discriminant s^2 - q never lose digits to cancellation.
+//
+// Sampler axes are built from texel coordinates. The reference maps a unit
+// value y to u = 0.5/N + y (1 - 1/N) (util.h:18-20) and the sampler takes
+// u N - 0.5, which is y (N - 1) exactly; evaluating y (N - 1) directly keeps
+// texel-centred lookups exactly on the texel (no spurious weight on a
+// neighbour that may be orders of magnitude larger).
+template <class T> __device__ __forceinline__ Axis axis_texel(T t, int n) {
+  T fl = floor(t);
+  Axis a;
+  a.f = (float)(t - fl);
+  fl = fl < T(-1) ? T(-1) : (fl > T(n) ? T(n) : fl);
+  if (!(fl == fl)) fl = T(-1);
+  int i = (int)fl;
+  a.i0 = min(max(i, 0), n - 1);
+  a.i1 = min(max(i + 1, 0), n - 1);
+  return a;
+}
+
+struct Geo64 {
+  double R, T, H, H2;
+  __device__ __forceinline__ void init(const DevAtmo& a) {
+    R = a.bottom;
+    T = a.top;
+    H2 = T * T - R * R;
+    H = sqrt(H2);
+  }
+  __device__ __forceinline__ double radius(double q) const { return sqrt(q + R * R); }
+  // params.h:105-110 with the discriminant T^2 - r^2 (1 - mu^2) = (H^2 - q) + s^2.
+  __device__ __forceinline__ double dist_top(double q, double s) const {
+    double e = H2 - q;  // T^2 - r^2
+    double root = sqrt(gmax(e + s * s, 0.0));
+    double d = s > 0.0 ? e / (s + root) : root - s;
+    return gmax(d, 0.0);
+  }
+  // params.h:112-117 with the discriminant s^2 - q.
+  __device__ __forceinline__ double dist_bottom(double q, double s) const {
+    double root = sqrt(gmax(s * s - q, 0.0));
+    double d = s < 0.0 ? q / (root - s) : -s - root;
+    return gmax(d, 0.0);
+  }
+  __device__ __forceinline__ bool hits_ground(double q, double s) const { return s < 0.0 && s * s - q >= 0.0; }
+  // ClampRadius on (q, s): r in [R, T] <=> q in [0, H^2]; mu in [-1, 1] <=> |s| <= r.
+  __device__ __forceinline__ void clamp_point(double& q, double& s) const {
+    q = gclamp(q, 0.0, H2);
+    double r = radius(q);
+    s = gclamp(s, -r, r);
+  }
+  // transmittance.h:7-24 as texel coordinates of the transmittance table.
+  __device__ __forceinline__ void tr_texel(const DevAtmo& a, double q, double s, double& tx, double& ty) const {
+    double rho = sqrt(gmax(q, 0.0));
+    double r = radius(q);
+    double d = dist_top(q, s);
+    double d_min = (H2 - q) / (T + r);
+    double d_max = rho + H;
+    tx = (d - d_min) / (d_max - d_min) * double(a.tr_mu - 1);
+    ty = rho / H * double(a.tr_r - 1);
+  }
+  __device__ __forceinline__ float3 tr_to_top(const DevAtmo& a, double q, double s) const {
+    double tx, ty;
+    tr_texel(a, q, s, tx, ty);
+    return fetch2(a.tr, a.tr_mu, axis_texel(tx, a.tr_mu), axis_texel(ty, a.tr_r));
+  }
+  // transmittance.h:35-61: transmittance from (q, s) over distance d.
+  __device__ __forceinline__ float3 tr_segment(const DevAtmo& a, double q, double s, double d, bool ground) const {
+    double qd = q + d * (2.0 * s + d), sd = s + d;
+    clamp_point(qd, sd);
+    float3 num, den;
+    if (ground) {
+      num = tr_to_top(a, qd, -sd);
+      den = tr_to_top(a, q, -s);
+    } else {
+      num = tr_to_top(a, q, s);
+      den = tr_to_top(a, qd, sd);
+    }
+    return min1(num / den);
+  }
+  // scattering.h:15-21: texel coordinate along r (depth of the 3D table).
+  __device__ __forceinline__ double sc_r_texel(const DevAtmo& a, double q) const {
+    return sqrt(gmax(q, 0.0)) / H * double(a.sc_r - 1);
+  }
+  // scattering.h:23-46: texel coordinate along mu (height of the 3D table).
+  // With M = mu_size / 2 the reference's u_mu maps to (M - 1)(1 - x) on the
+  // ground half and M + x (M - 1) on the sky half.
+  __device__ __forceinline__ double sc_mu_texel(const DevAtmo& a, double q, double s, bool ground) const {
+    const int M = a.sc_mu / 2;
+    double rho = sqrt(gmax(q, 0.0));
+    double r = radius(q);
+    if (ground) {
+      double d = dist_bottom(q, s);
+      double d_min = q / (r + R);
+      double d_max = rho;
+      double x = d_max == d_min ? 0.0 : (d - d_min) / (d_max - d_min);
+      return double(M - 1) * (1.0 - x);
+    }
+    double d = dist_top(q, s);
+    double d_min = (H2 - q) / (T + r);
+    double d_max = rho + H;
+    double x = (d - d_min) / (d_max - d_min);
+    return double(M) + x * double(M - 1);
+  }
+  // scattering.h:48-56: the unit-range mu_s value y (texel coordinate within a
+  // nu slice is y (mu_s_size - 1)). The distance from the ground to the top
+  // along mu_s is H^2 / (s + sqrt(s^2 + H^2)) with s = R mu_s.
+  __device__ __forceinline__ double mus_unit(const DevAtmo& a, double mu_s) const {
+    double s = R * mu_s;
+    double root = sqrt(s * s + H2);
+    double d = s > 0.0 ? H2 / (s + root) : root - s;
+    double d_min = T - R;
+    double d_max = H;
+    double aa = (d - d_min) / (d_max - d_min);
+    double A = -2.0 * a.mu_s_min * R / (d_max - d_min);
+    return gmax(1.0 - aa / A, 0.0) / (1.0 + aa);
+  }
+};
+
+// FP32 form of Geo64::mus_unit for per-texel-sample use in the mixed mode: the
+// same cancellation-free distance, single precision, constants precomputed.
+struct MuS32 {
+  float R, H2, dmin, inv_span, inv_A, scale;
+  __device__ __forceinline__ void init(const DevAtmo& a) {
+    const double Rd = a.bottom, Td = a.top;
+    const double H2d = Td * Td - Rd * Rd;
+    const double span = sqrt(H2d) - (Td - Rd);
+    R = a.bottom;
+    H2 = (float)H2d;
+    dmin = (float)(Td - Rd);
+    inv_span = (float)(1.0 / span);
+    inv_A = (float)(span / (-2.0 * a.mu_s_min * Rd));
+    scale = float(a.sc_mus - 1);
+  }
+  // texel coordinate within a nu slice
+  __device__ __forceinline__ float texel(float mu_s) const {
+    float s = R * mu_s;
+    float root = sqrtf(fmaf(s, s, H2));
+    float d = s > 0.0f ? H2 / (s + root) : root - s;
+    float aa = (d - dmin) * inv_span;
+    return gmax(1.0f - aa * inv_A, 0.0f) / (1.0f + aa) * scale;
+  }
+};
+
+// --------------------------------------------------------- texel decoding
+// scattering.h:62-137 + util.h:36-45: texel (x, y, z) of the packed 3D table
+// to (r, mu, mu_s, nu, ground), nu clamped to its valid range.
+struct TexelParams {
+  double r, mu, mu_s, nu, q, s;  // q = r^2 - R^2, s = r mu
+  bool ground;
+};
+
+// PLAIN: the reference's float arithmetic.
+__device__ __forceinline__ void decode_texel32(const DevAtmo& a, const Geo32& G, uint32_t ix, uint32_t iy,
+                                               uint32_t iz, float& r, float& mu, float& mu_s, float& nu,
+                                               bool& ground) {
+  const uint32_t W = (uint32_t)a.W;
+  float fx = frag_from_texel(ix, W), fy = frag_from_texel(iy, (uint32_t)a.sc_mu),
+        fz = frag_from_texel(iz, (uint32_t)a.sc_r);
+  float nmus = float(a.sc_mus);
+  float f_nu = floorf(fx / nmus);
+  float f_mus = fx - nmus * floorf(fx / nmus);
+  float qx = f_nu / float(a.sc_nu - 1), qy = f_mus / nmus, qz = fy / float(a.sc_mu), qw = fz / float(a.sc_r);
+  float rho = G.H * unit_from_coord(qw, a.sc_r);
+  r = sqrtf(rho * rho + G.R * G.R);
+  if (qz < 0.5f) {
+    float d_min = r - G.R;
+    float d_max = rho;
+    float d = d_min + (d_max - d_min) * unit_from_coord(1.0f - 2.0f * qz, a.sc_mu / 2);
+    mu = d == 0.0f ? -1.0f : clamp_cosine(-(rho * rho + d * d) / (2.0f * r * d));
+    ground = true;
+  } else {
+    float d_min = G.T - r;
+    float d_max = rho + G.H;
+    float d = d_min + (d_max - d_min) * unit_from_coord(2.0f * qz - 1.0f, a.sc_mu / 2);
+    mu = d == 0.0f ? 1.0f : clamp_cosine((G.H * G.H - rho * rho - d * d) / (2.0f * r * d));
+    ground = false;
+  }
+  float x_mu_s = unit_from_coord(qy, a.sc_mus);
+  float d_min = G.T - G.R;
+  float d_max = G.H;
+  float A = -2.0f * a.mu_s_min * G.R / (d_max - d_min);
+  float aa = (A - x_mu_s * A) / (1.0f + x_mu_s * A);
+  float d = d_min + gmin(aa, A) * (d_max - d_min);
+  mu_s = d == 0.0f ? 1.0f : clamp_cosine((G.H * G.H - d * d) / (2.0f * G.R * d));
+  nu = clamp_cosine(qx * 2.0f - 1.0f);
+  float sq = sqrtf((1.0f - mu * mu) * (1.0f - mu_s * mu_s));
+  nu = gclamp(nu, mu * mu_s - sq, mu * mu_s + sq);
+}
+
+// MIXED: the same decode in FP64, producing q and s directly.
+__device__ __forceinline__ TexelParams decode_texel64(const DevAtmo& a, const Geo64& G, uint32_t ix, uint32_t iy,
+                                                      uint32_t iz) {
+  TexelParams o;
+  const uint32_t W = (uint32_t)a.W;
+  double fx = frag_from_texel_d(ix, W), fy = frag_from_texel_d(iy, (uint32_t)a.sc_mu),
+         fz = frag_from_texel_d(iz, (uint32_t)a.sc_r);
+  double nmus = double(a.sc_mus);
+  double f_nu = floor(fx / nmus);
+  double f_mus = fx - nmus * floor(fx / nmus);
+  double qx = f_nu / double(a.sc_nu - 1), qy = f_mus / nmus, qz = fy / double(a.sc_mu), qw = fz / double(a.sc_r);
+  double rho = G.H * unit_from_coord(qw, a.sc_r);
+  o.q = rho * rho;
+  o.r = G.radius(o.q);
+  if (qz < 0.5) {
+    double d_min = o.q / (o.r + G.R);
+    double d_max = rho;
+    double d = d_min + (d_max - d_min) * unit_from_coord(1.0 - 2.0 * qz, a.sc_mu / 2);
+    o.s = d == 0.0 ? -o.r : gmax(-(o.q + d * d) / (2.0 * d), -o.r);
+    o.ground = true;
+  } else {
+    double d_min = (G.H2 - o.q) / (G.T + o.r);
+    double d_max = rho + G.H;
+    double d = d_min + (d_max - d_min) * unit_from_coord(2.0 * qz - 1.0, a.sc_mu / 2);
+    o.s = d == 0.0 ? o.r : gclamp((G.H2 - o.q - d * d) / (2.0 * d), -o.r, o.r);
+    o.ground = false;
+  }
+  o.mu = o.s / o.r;
+  double x_mu_s = unit_from_coord(qy, a.sc_mus);
+  double d_min = G.T - G.R;
+  double d_max = G.H;
+  double A = -2.0 * a.mu_s_min * G.R / (d_max - d_min);
+  double aa = (A - x_mu_s * A) / (1.0 + x_mu_s * A);
+  double d = d_min + gmin(aa, A) * (d_max - d_min);
+  o.mu_s = d == 0.0 ? 1.0 : clamp_cosine((G.H2 - d * d) / (2.0 * G.R * d));
+  double nu = clamp_cosine(qx * 2.0 - 1.0);
+  double sq = sqrt((1.0 - o.mu * o.mu) * (1.0 - o.mu_s * o.mu_s));
+  o.nu = gclamp(nu, o.mu * o.mu_s - sq, o.mu * o.mu_s + sq);
+  return o;
+}
+
+}  // namespace fb

@@ -1,0 +1,54 @@
+// fb_internal.h — declarations shared by the host-side translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <vector>
+
+#include "../../include/fuzzyblue.h"
+
+namespace fbi {
+
+struct TableSizes {
+  size_t ntr, nir, nsc;   // texels
+  size_t out_bytes;       // transmittance + irradiance + scattering
+  size_t tmp_bytes;       // temporaries of one build
+};
+TableSizes sizes_of(const fb_params& p);
+
+// Tile shapes per scattering-table class, chosen by the autotuner
+// (fb_builder_autotune) or by the default rule.
+struct TuneEntry {
+  int sc_r, sc_mu, sc_mus, sc_nu;
+  int density_chunk;
+};
+struct Tuning {
+  std::vector<TuneEntry> entries;
+};
+void tuning_load_default(Tuning& t);
+int tuning_density_chunk(const Tuning& t, int sc_r, int sc_mu, int sc_mus, int sc_nu);
+int default_density_chunk(int sc_mu, int sc_nu);
+
+void builder_ref(fb_builder* b);
+void builder_unref(fb_builder* b);
+void* dev_alloc(fb_builder* b, size_t bytes, cudaStream_t s);
+void dev_free(fb_builder* b, void* p, cudaStream_t s);
+int builder_sms(const fb_builder* b);
+int builder_device(const fb_builder* b);
+cudaStream_t builder_stream(const fb_builder* b);
+Tuning& builder_tuning(fb_builder* b);
+std::mutex& builder_mutex(fb_builder* b);
+int set_error(int code, const char* msg);
+
+fb_atmosphere* atmosphere_new(fb_builder* b, const fb_params& p, cudaStream_t s);
+void atmosphere_free(fb_atmosphere* a);
+const fb_params& atmosphere_params(const fb_atmosphere* a);
+void atmosphere_set_stream(fb_atmosphere* a, cudaStream_t s);
+void atmosphere_tables(const fb_atmosphere* a, float4** tr, float4** ir, float4** sc);
+
+int build(fb_builder* b, cudaStream_t s, const fb_params* params, uint32_t count, bool use_graph, fb_pending** out);
+void pending_destroy(fb_pending* p);
+
+cudaError_t launch_to_half(const float4* src, void* dst, size_t n, cudaStream_t s);
+
+}  // namespace fbi

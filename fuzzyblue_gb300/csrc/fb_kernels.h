@@ -1,0 +1,25 @@
+// fb_kernels.h — host-side entry points of the pass kernels (internal).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "fb_passes.cuh"
+
+namespace fb {
+
+enum PassKind { kPassTransmittance = 0, kPassSingle = 1, kPassDensity = 2, kPassMultiple = 3 };
+
+// Kernel of (mode, pass, texels-per-thread); tpt is used by kPassMultiple only
+// (1, 2, 4 or 8).
+const void* kernel_plain(int pass, int tpt);
+const void* kernel_mixed(int pass, int tpt);
+
+inline const void* kernel_for(bool mixed, int pass, int tpt) {
+  return mixed ? kernel_mixed(pass, tpt) : kernel_plain(pass, tpt);
+}
+
+inline int tpt_for_width(int W) {
+  const int n = (W + kThreads - 1) / kThreads;
+  return n <= 1 ? 1 : n <= 2 ? 2 : n <= 4 ? 4 : 8;
+}
+
+}  // namespace fb

@@ -139,9 +139,15 @@ typedef struct fb_extent {
  * extension fields. */
 void fb_params_default(fb_params* out);
 
-/* Checks sizes and geometry; FB_OK or FB_ERR_INVALID_PARAMS. Sizes must be
- * >= 2, scattering_mu_size even, top_radius > bottom_radius > 0, order >= 1,
- * sample counts within [1, 4096] (density/irradiance samples even, <= 64). */
+/* Checks sizes and geometry; FB_OK or FB_ERR_INVALID_PARAMS (the reason is in
+ * fb_last_error). Rules: every table size in [2, 65536]; scattering_mu_size
+ * even; scattering_nu_size <= 64; nu_size * mu_s_size <= 2048; irradiance
+ * mu_s size <= 4096; 0 < bottom_radius < top_radius; order in [1, 64];
+ * transmittance_steps in [1, 1e6]; single/multiple scattering steps in
+ * [1, 1024]; density_samples even in [2, 32]; irradiance_samples even in
+ * [2, 64]; known precision and storage modes. The reference silently leaves
+ * texels unwritten for sizes that are not multiples of its workgroup size
+ * (src/precompute.rs:1742,1797); every size accepted here is computed fully. */
 int fb_params_validate(const fb_params* p);
 
 /* Parameters::{transmittance,irradiance,scattering}_extent
@@ -169,7 +175,9 @@ int fb_builder_sm_count(const fb_builder* b, int* sms);
 
 /* Host-side allocation hook: when set, every device allocation the builder
  * makes goes through `alloc` (return NULL to report failure) and `release`.
- * Used to inject allocation failures in tests; NULL restores cudaMallocAsync. */
+ * Used to inject allocation failures in tests; NULL restores the builder's own
+ * stream-ordered memory pool (cudaMallocFromPoolAsync on a pool that keeps
+ * freed memory for reuse). */
 typedef void* (*fb_alloc_fn)(void* user, size_t bytes, void* stream);
 typedef void (*fb_free_fn)(void* user, void* ptr, void* stream);
 int fb_builder_set_allocator(fb_builder* b, fb_alloc_fn alloc, fb_free_fn release,
@@ -199,6 +207,19 @@ int fb_pending_atmosphere(fb_pending* p, uint32_t index, fb_atmosphere** out);
 /* Transfers ownership of atmosphere `index` to the caller (who then calls
  * fb_atmosphere_destroy). Waits for completion first. */
 int fb_pending_take(fb_pending* p, uint32_t index, fb_atmosphere** out);
+/* Device pointers of the temporaries of atmosphere `index` (the images
+ * PendingAtmosphere owns, src/precompute.rs:2111-2121), valid until
+ * fb_pending_release. After the build they hold the values of the last order:
+ * delta_irradiance[n & 1] the irradiance read by order n's density,
+ * delta_irradiance[(n+1) & 1] the indirect irradiance of order n-1. */
+typedef struct fb_intermediates {
+    void* delta_irradiance[2];
+    void* delta_rayleigh;
+    void* delta_mie;
+    void* delta_multiple_scattering;
+    void* scattering_density;
+} fb_intermediates;
+int fb_pending_intermediates(fb_pending* p, uint32_t index, fb_intermediates* out);
 /* Drop for PendingAtmosphere (src/precompute.rs:2122-2140): frees the
  * temporaries (stream-ordered) and every atmosphere not taken. */
 void fb_pending_release(fb_pending* p);
@@ -237,6 +258,35 @@ void fb_atmosphere_destroy(fb_atmosphere* a);
  * fb_pending_atmosphere(p, i, ...). */
 int fb_batch_build(fb_builder* b, void* stream, const fb_params* params,
                    uint32_t count, fb_pending** out);
+
+/* ---- profiling ----------------------------------------------------------- */
+
+/* When enabled, builds record a CUDA timing event around every kernel launch
+ * (captured into the graph for batches); fb_pending_profile then reports the
+ * device time of each launch once the build has completed. */
+int fb_builder_set_profiling(fb_builder* b, int enabled);
+
+#define FB_KERNEL_TRANSMITTANCE 0 /* transmittance.comp */
+#define FB_KERNEL_SINGLE 1        /* single_scattering + direct_irradiance */
+#define FB_KERNEL_DENSITY 2       /* scattering_density + indirect_irradiance */
+#define FB_KERNEL_MULTIPLE 3      /* multiple_scattering */
+
+typedef struct fb_launch_profile {
+    uint32_t kernel;     /* FB_KERNEL_* */
+    uint32_t order;      /* scattering order of the launch (0 for the first two) */
+    uint32_t precision;  /* FB_PRECISION_* */
+    uint32_t grid;       /* CTAs launched (persistent) */
+    uint64_t items;      /* work items (tiles) processed */
+    uint64_t texels;     /* output texels written by the launch */
+    float ms;            /* device time */
+    float _pad;
+} fb_launch_profile;
+
+/* Copies up to `capacity` launch records into `out` and sets *count to the
+ * number of launches of the build. Waits for the build. FB_ERR_NOT_FOUND if
+ * profiling was off when the build was enqueued. */
+int fb_pending_profile(fb_pending* p, fb_launch_profile* out, uint32_t capacity,
+                       uint32_t* count);
 
 /* ---- diagnostics --------------------------------------------------------- */
 

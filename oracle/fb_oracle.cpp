@@ -70,6 +70,7 @@ template <class T> struct Atmo {
   int tr_mu, tr_r, sc_r, sc_mu, sc_mus, sc_nu, ir_mus, ir_r;
   int tr_steps, ss_steps, ms_steps, dens_n, irr_n, order;
   bool f16;
+  bool exact_altitude;  // FP64 oracle: clamp rounding-negative altitudes (see optical_length)
 };
 
 template <class T> V3<T> v3(const float* f) { return V3<T>(T(f[0]), T(f[1]), T(f[2])); }
@@ -119,6 +120,7 @@ template <class T> Atmo<T> load(const fb_params* p) {
   a.irr_n = (int)p->irradiance_samples;
   a.order = (int)p->order;
   a.f16 = p->storage == FB_STORAGE_F16;
+  a.exact_altitude = sizeof(T) == sizeof(double);
   return a;
 }
 
@@ -412,7 +414,14 @@ template <class T> T optical_length(const Atmo<T>& a, const Profile<T>& P, T r, 
   for (int i = 0; i <= N; ++i) {
     T d_i = T(i) * dx;
     T r_i = Num<T>::sqrt(d_i * d_i + T(2) * r * mu * d_i + r * r);
-    T y_i = profile_density(P, r_i - a.bottom);
+    T h_i = r_i - a.bottom;
+    // Every ray of the transmittance table stays above the ground in exact
+    // arithmetic (mu is at or above the horizon), so a negative altitude is a
+    // rounding artefact; the FP64 oracle evaluates the exact-arithmetic value
+    // (h = 0 at a tangent sample). The FP32 oracle keeps the reference's
+    // unclamped arithmetic.
+    if (a.exact_altitude && h_i < T(0)) h_i = T(0);
+    T y_i = profile_density(P, h_i);
     T w = (i == 0 || i == N) ? T(0.5) : T(1);
     result = result + y_i * w * dx;
   }
@@ -693,6 +702,53 @@ int multiple_impl(const fb_params* p, int nthreads, const T* tr, const T* dens, 
   return FB_OK;
 }
 
+template <class T> int transmittance_impl(const fb_params* p, int nthreads, const int64_t* idx, int64_t n, T* out) {
+  if (!valid(p) || !out) return FB_ERR_INVALID_ARGUMENT;
+  Threads th(nthreads);
+  const Atmo<T> a = load<T>(p);
+  if (!idx) n = (int64_t)a.tr_mu * a.tr_r;
+  for_texels(idx, n, [&](int64_t k, int64_t t) { transmittance_texel(a, t, out + 4 * k); });
+  return FB_OK;
+}
+
+template <class T>
+int direct_impl(const fb_params* p, int nthreads, const T* tr, const int64_t* idx, int64_t n, T* out) {
+  if (!valid(p) || !out || !tr) return FB_ERR_INVALID_ARGUMENT;
+  Threads th(nthreads);
+  const Atmo<T> a = load<T>(p);
+  if (!idx) n = (int64_t)a.ir_mus * a.ir_r;
+  const Tab<T> t = tab<T>(tr, a.tr_mu, a.tr_r);
+  for_texels(idx, n, [&](int64_t k, int64_t x) { direct_irradiance_texel(a, t, x, out + 4 * k); });
+  return FB_OK;
+}
+
+template <class T>
+int single_impl(const fb_params* p, int nthreads, const T* tr, const int64_t* idx, int64_t n, T* out_r, T* out_m) {
+  if (!valid(p) || !tr || !out_r || !out_m) return FB_ERR_INVALID_ARGUMENT;
+  Threads th(nthreads);
+  const Atmo<T> a = load<T>(p);
+  if (!idx) n = (int64_t)a.sc_nu * a.sc_mus * a.sc_mu * a.sc_r;
+  const Tab<T> t = tab<T>(tr, a.tr_mu, a.tr_r);
+  for_texels(idx, n, [&](int64_t k, int64_t x) { single_scattering_texel(a, t, x, out_r + 4 * k, out_m + 4 * k); });
+  return FB_OK;
+}
+
+template <class T>
+int indirect_impl(const fb_params* p, int nthreads, int order, const T* sr, const T* sm, const T* ms,
+                  const int64_t* idx, int64_t n, T* out) {
+  if (!valid(p) || !out || order < 1) return FB_ERR_INVALID_ARGUMENT;
+  if (order == 1 && (!sr || !sm)) return FB_ERR_INVALID_ARGUMENT;
+  if (order > 1 && !ms) return FB_ERR_INVALID_ARGUMENT;
+  Threads th(nthreads);
+  const Atmo<T> a = load<T>(p);
+  const int W = a.sc_nu * a.sc_mus;
+  if (!idx) n = (int64_t)a.ir_mus * a.ir_r;
+  const Tab<T> tsr = tab<T>(sr ? sr : ms, W, a.sc_mu, a.sc_r), tsm = tab<T>(sm ? sm : ms, W, a.sc_mu, a.sc_r);
+  const Tab<T> tms = tab<T>(ms ? ms : sr, W, a.sc_mu, a.sc_r);
+  for_texels(idx, n, [&](int64_t k, int64_t x) { indirect_texel(a, order, tsr, tsm, tms, x, out + 4 * k); });
+  return FB_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -707,36 +763,27 @@ int fbo_precompute_f64(const fb_params* p, int nthreads, double* tr, double* ir,
 }
 
 int fbo_transmittance_f32(const fb_params* p, int nthreads, const int64_t* idx, int64_t n, float* out) {
-  if (!valid(p) || !out) return FB_ERR_INVALID_ARGUMENT;
-  Threads th(nthreads);
-  const Atmo<float> a = load<float>(p);
-  if (!idx) n = (int64_t)a.tr_mu * a.tr_r;
-  for_texels(idx, n, [&](int64_t k, int64_t t) { transmittance_texel(a, t, out + 4 * k); });
-  return FB_OK;
+  return transmittance_impl<float>(p, nthreads, idx, n, out);
 }
-
-int fbo_direct_irradiance_f32(const fb_params* p, int nthreads, const float* tr, const int64_t* idx,
-                              int64_t n, float* out) {
-  if (!valid(p) || !out || !tr) return FB_ERR_INVALID_ARGUMENT;
-  Threads th(nthreads);
-  const Atmo<float> a = load<float>(p);
-  if (!idx) n = (int64_t)a.ir_mus * a.ir_r;
-  const Tab<float> t = tab<float>(tr, a.tr_mu, a.tr_r);
-  for_texels(idx, n, [&](int64_t k, int64_t x) { direct_irradiance_texel(a, t, x, out + 4 * k); });
-  return FB_OK;
+int fbo_transmittance_f64(const fb_params* p, int nthreads, const int64_t* idx, int64_t n, double* out) {
+  return transmittance_impl<double>(p, nthreads, idx, n, out);
 }
-
-int fbo_single_scattering_f32(const fb_params* p, int nthreads, const float* tr, const int64_t* idx,
-                              int64_t n, float* out_r, float* out_m) {
-  if (!valid(p) || !tr || !out_r || !out_m) return FB_ERR_INVALID_ARGUMENT;
-  Threads th(nthreads);
-  const Atmo<float> a = load<float>(p);
-  if (!idx) n = (int64_t)a.sc_nu * a.sc_mus * a.sc_mu * a.sc_r;
-  const Tab<float> t = tab<float>(tr, a.tr_mu, a.tr_r);
-  for_texels(idx, n, [&](int64_t k, int64_t x) { single_scattering_texel(a, t, x, out_r + 4 * k, out_m + 4 * k); });
-  return FB_OK;
+int fbo_direct_irradiance_f32(const fb_params* p, int nthreads, const float* tr, const int64_t* idx, int64_t n,
+                              float* out) {
+  return direct_impl<float>(p, nthreads, tr, idx, n, out);
 }
-
+int fbo_direct_irradiance_f64(const fb_params* p, int nthreads, const double* tr, const int64_t* idx, int64_t n,
+                              double* out) {
+  return direct_impl<double>(p, nthreads, tr, idx, n, out);
+}
+int fbo_single_scattering_f32(const fb_params* p, int nthreads, const float* tr, const int64_t* idx, int64_t n,
+                              float* out_r, float* out_m) {
+  return single_impl<float>(p, nthreads, tr, idx, n, out_r, out_m);
+}
+int fbo_single_scattering_f64(const fb_params* p, int nthreads, const double* tr, const int64_t* idx, int64_t n,
+                              double* out_r, double* out_m) {
+  return single_impl<double>(p, nthreads, tr, idx, n, out_r, out_m);
+}
 
 int fbo_scattering_density_f32(const fb_params* p, int nthreads, int order, const float* tr, const float* sr,
                                const float* sm, const float* ms, const float* dirr, const int64_t* idx,
@@ -751,17 +798,11 @@ int fbo_scattering_density_f64(const fb_params* p, int nthreads, int order, cons
 
 int fbo_indirect_irradiance_f32(const fb_params* p, int nthreads, int order, const float* sr, const float* sm,
                                 const float* ms, const int64_t* idx, int64_t n, float* out) {
-  if (!valid(p) || !out || order < 1) return FB_ERR_INVALID_ARGUMENT;
-  if (order == 1 && (!sr || !sm)) return FB_ERR_INVALID_ARGUMENT;
-  if (order > 1 && !ms) return FB_ERR_INVALID_ARGUMENT;
-  Threads th(nthreads);
-  const Atmo<float> a = load<float>(p);
-  const int W = a.sc_nu * a.sc_mus;
-  if (!idx) n = (int64_t)a.ir_mus * a.ir_r;
-  const Tab<float> tsr = tab<float>(sr ? sr : ms, W, a.sc_mu, a.sc_r), tsm = tab<float>(sm ? sm : ms, W, a.sc_mu, a.sc_r);
-  const Tab<float> tms = tab<float>(ms ? ms : sr, W, a.sc_mu, a.sc_r);
-  for_texels(idx, n, [&](int64_t k, int64_t x) { indirect_texel(a, order, tsr, tsm, tms, x, out + 4 * k); });
-  return FB_OK;
+  return indirect_impl<float>(p, nthreads, order, sr, sm, ms, idx, n, out);
+}
+int fbo_indirect_irradiance_f64(const fb_params* p, int nthreads, int order, const double* sr, const double* sm,
+                                const double* ms, const int64_t* idx, int64_t n, double* out) {
+  return indirect_impl<double>(p, nthreads, order, sr, sm, ms, idx, n, out);
 }
 
 int fbo_multiple_scattering_f32(const fb_params* p, int nthreads, const float* tr, const float* dens,

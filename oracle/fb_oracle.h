@@ -11,7 +11,11 @@
  *   _f32  IEEE single precision, no FMA contraction: the arithmetic of the
  *         reference's GLSL (float literals, float intermediates), with exact
  *         bilinear/trilinear weights in place of the sampler's fixed-point ones.
- *   _f64  the same integrals in double precision: the accuracy oracle.
+ *   _f64  the same integrals in double precision: the accuracy oracle. In the
+ *         transmittance march it evaluates the exact-arithmetic altitude of
+ *         samples that rounding puts a hair below the ground (every ray of that
+ *         table stays at or above the ground), so that tangent samples do not
+ *         flip the width-0 layer test of params.h:95-99 at random.
  *
  * Texel layout of every table: RGBA (4 values per texel), x fastest, then y,
  * then z, exactly like the library's tables.
@@ -75,6 +79,18 @@ int fbo_multiple_scattering_f32(const fb_params* p, int nthreads,
                                 float* out_phase);
 
 /* Same single passes in double precision (inputs and outputs double). */
+int fbo_transmittance_f64(const fb_params* p, int nthreads, const int64_t* idx,
+                          int64_t n, double* out);
+int fbo_direct_irradiance_f64(const fb_params* p, int nthreads,
+                              const double* transmittance, const int64_t* idx,
+                              int64_t n, double* out);
+int fbo_single_scattering_f64(const fb_params* p, int nthreads,
+                              const double* transmittance, const int64_t* idx,
+                              int64_t n, double* out_rayleigh, double* out_mie);
+int fbo_indirect_irradiance_f64(const fb_params* p, int nthreads, int order,
+                                const double* single_r, const double* single_m,
+                                const double* multiple, const int64_t* idx,
+                                int64_t n, double* out);
 int fbo_scattering_density_f64(const fb_params* p, int nthreads, int order,
                                const double* transmittance, const double* single_r,
                                const double* single_m, const double* multiple,

@@ -38,8 +38,12 @@ def lib():
         L.fbo_precompute_f32.argtypes = [P, ctypes.c_int] + [_F] * 7
         L.fbo_precompute_f64.argtypes = [P, ctypes.c_int] + [_D] * 7
         L.fbo_transmittance_f32.argtypes = [P, ctypes.c_int, _I, ctypes.c_int64, _F]
+        L.fbo_transmittance_f64.argtypes = [P, ctypes.c_int, _I, ctypes.c_int64, _D]
         L.fbo_direct_irradiance_f32.argtypes = [P, ctypes.c_int, _F, _I, ctypes.c_int64, _F]
+        L.fbo_direct_irradiance_f64.argtypes = [P, ctypes.c_int, _D, _I, ctypes.c_int64, _D]
         L.fbo_single_scattering_f32.argtypes = [P, ctypes.c_int, _F, _I, ctypes.c_int64, _F, _F]
+        L.fbo_single_scattering_f64.argtypes = [P, ctypes.c_int, _D, _I, ctypes.c_int64, _D, _D]
+        L.fbo_indirect_irradiance_f64.argtypes = [P, ctypes.c_int, ctypes.c_int] + [_D] * 3 + [_I, ctypes.c_int64, _D]
         L.fbo_scattering_density_f32.argtypes = [P, ctypes.c_int, ctypes.c_int] + [_F] * 5 + [_I, ctypes.c_int64, _F]
         L.fbo_scattering_density_f64.argtypes = [P, ctypes.c_int, ctypes.c_int] + [_D] * 5 + [_I, ctypes.c_int64, _D]
         L.fbo_indirect_irradiance_f32.argtypes = [P, ctypes.c_int, ctypes.c_int] + [_F] * 3 + [_I, ctypes.c_int64, _F]
@@ -127,32 +131,41 @@ def _idx(idx):
     return a, a.size
 
 
-def transmittance(p, idx=None, nthreads=0):
+def _kind(dtype):
+    return (_F, "f32") if np.dtype(dtype) == np.float32 else (_D, "f64")
+
+
+def transmittance(p, idx=None, nthreads=0, dtype=np.float32):
     a, n = _idx(idx)
+    kind, sfx = _kind(dtype)
     cnt = n if a is not None else p.texel_counts()[0]
-    out = np.zeros((cnt, 4), np.float32)
-    _check(lib().fbo_transmittance_f32(ctypes.byref(p.to_c()), nthreads, _ptr(a, _I), n, _ptr(out, _F)), "transmittance")
+    out = np.zeros((cnt, 4), dtype)
+    fn = getattr(lib(), "fbo_transmittance_" + sfx)
+    _check(fn(ctypes.byref(p.to_c()), nthreads, _ptr(a, _I), n, _ptr(out, kind)), "transmittance")
     return out
 
 
-def direct_irradiance(p, tr, idx=None, nthreads=0):
+def direct_irradiance(p, tr, idx=None, nthreads=0, dtype=np.float32):
     a, n = _idx(idx)
+    kind, sfx = _kind(dtype)
     cnt = n if a is not None else p.texel_counts()[1]
-    out = np.zeros((cnt, 4), np.float32)
-    tr = np.ascontiguousarray(tr, np.float32)
-    _check(lib().fbo_direct_irradiance_f32(ctypes.byref(p.to_c()), nthreads, _ptr(tr, _F), _ptr(a, _I), n,
-                                           _ptr(out, _F)), "direct_irradiance")
+    out = np.zeros((cnt, 4), dtype)
+    tr = np.ascontiguousarray(tr, dtype)
+    fn = getattr(lib(), "fbo_direct_irradiance_" + sfx)
+    _check(fn(ctypes.byref(p.to_c()), nthreads, _ptr(tr, kind), _ptr(a, _I), n, _ptr(out, kind)), "direct_irradiance")
     return out
 
 
-def single_scattering(p, tr, idx=None, nthreads=0):
+def single_scattering(p, tr, idx=None, nthreads=0, dtype=np.float32):
     a, n = _idx(idx)
+    kind, sfx = _kind(dtype)
     cnt = n if a is not None else p.texel_counts()[2]
-    r = np.zeros((cnt, 4), np.float32)
-    m = np.zeros((cnt, 4), np.float32)
-    tr = np.ascontiguousarray(tr, np.float32)
-    _check(lib().fbo_single_scattering_f32(ctypes.byref(p.to_c()), nthreads, _ptr(tr, _F), _ptr(a, _I), n,
-                                           _ptr(r, _F), _ptr(m, _F)), "single_scattering")
+    r = np.zeros((cnt, 4), dtype)
+    m = np.zeros((cnt, 4), dtype)
+    tr = np.ascontiguousarray(tr, dtype)
+    fn = getattr(lib(), "fbo_single_scattering_" + sfx)
+    _check(fn(ctypes.byref(p.to_c()), nthreads, _ptr(tr, kind), _ptr(a, _I), n, _ptr(r, kind), _ptr(m, kind)),
+           "single_scattering")
     return r, m
 
 
@@ -169,13 +182,15 @@ def scattering_density(p, order, tr, single_r, single_m, multiple, delta_irr, id
     return out
 
 
-def indirect_irradiance(p, order, single_r, single_m, multiple, idx=None, nthreads=0):
+def indirect_irradiance(p, order, single_r, single_m, multiple, idx=None, nthreads=0, dtype=np.float32):
     a, n = _idx(idx)
+    kind, sfx = _kind(dtype)
     cnt = n if a is not None else p.texel_counts()[1]
-    out = np.zeros((cnt, 4), np.float32)
-    conv = [None if x is None else np.ascontiguousarray(x, np.float32) for x in (single_r, single_m, multiple)]
-    _check(lib().fbo_indirect_irradiance_f32(ctypes.byref(p.to_c()), nthreads, order, *[_ptr(x, _F) for x in conv],
-                                             _ptr(a, _I), n, _ptr(out, _F)), "indirect_irradiance")
+    out = np.zeros((cnt, 4), dtype)
+    conv = [None if x is None else np.ascontiguousarray(x, dtype) for x in (single_r, single_m, multiple)]
+    fn = getattr(lib(), "fbo_indirect_irradiance_" + sfx)
+    _check(fn(ctypes.byref(p.to_c()), nthreads, order, *[_ptr(x, kind) for x in conv], _ptr(a, _I), n,
+              _ptr(out, kind)), "indirect_irradiance")
     return out
 
 

@@ -1,0 +1,100 @@
+"""The C ABI: the library loads without a GPU, exports every symbol the
+header declares, and its parameter handling matches the reference's layout and
+defaults. No call here touches a GPU."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from fuzzyblue_gb300.params import Parameters, c_params, c_params_raw, smoke_parameters
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    text = open(os.path.join(ROOT, "include", "fuzzyblue.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(fb_[a-z0-9_]+)\s*\(", text)) - {"fb_alloc_fn", "fb_free_fn"})
+
+
+def test_library_exports_every_declared_symbol(native_lib):
+    syms = declared_symbols()
+    assert len(syms) >= 25
+    missing = [s for s in syms if not hasattr(native_lib, s)]
+    assert not missing, missing
+
+
+def test_python_bindings_cover_header(native_lib):
+    from fuzzyblue_gb300 import _native
+    assert set(declared_symbols()) <= set(_native.SIGNATURES), set(declared_symbols()) - set(_native.SIGNATURES)
+
+
+def test_params_raw_is_the_std140_block():
+    # ParamsRaw, src/precompute.rs:937-964: 320 bytes, profiles at 128/192/256
+    assert ctypes.sizeof(c_params_raw) == 320
+    assert c_params_raw.transmittance_mu_size.offset == 92
+    assert c_params_raw.rayleigh_density.offset == 128
+    assert c_params_raw.mie_density.offset == 192
+    assert c_params_raw.absorption_density.offset == 256
+    assert ctypes.sizeof(c_params) == 384
+
+
+def test_default_params_match_library(native_lib):
+    c = c_params()
+    native_lib.fb_params_default(ctypes.byref(c))
+    assert bytes(c) == bytes(Parameters().to_c())
+
+
+def test_extents_and_bytes(native_lib):
+    from fuzzyblue_gb300 import _native as N
+    p = Parameters()
+    c = p.to_c()
+    e = [N.c_extent() for _ in range(3)]
+    assert native_lib.fb_params_extents(ctypes.byref(c), *[ctypes.byref(x) for x in e]) == 0
+    assert (e[0].width, e[0].height) == p.transmittance_extent() == (256, 64)
+    assert (e[1].width, e[1].height) == p.irradiance_extent() == (64, 16)
+    assert (e[2].width, e[2].height, e[2].depth) == p.scattering_extent() == (256, 128, 32)
+    o, t = ctypes.c_uint64(), ctypes.c_uint64()
+    assert native_lib.fb_params_device_bytes(ctypes.byref(c), ctypes.byref(o), ctypes.byref(t)) == 0
+    assert o.value >= 16 * (256 * 64 + 64 * 16 + 256 * 128 * 32)
+    assert t.value >= 16 * 4 * 256 * 128 * 32
+
+
+@pytest.mark.parametrize("bad", [
+    dict(scattering_mu_size=31),            # odd mu size (the ground/sky split needs halves)
+    dict(scattering_nu_size=1),             # nu decode divides by nu_size - 1
+    dict(transmittance_mu_size=1),
+    dict(top_radius=6000.0),                # top below bottom
+    dict(order=0),
+    dict(density_samples=15),
+    dict(density_samples=34),
+    dict(irradiance_samples=66),
+    dict(single_scattering_steps=0),
+    dict(multiple_scattering_steps=2000),
+    dict(scattering_nu_size=64, scattering_mu_s_size=64),  # packed width > 2048
+    dict(precision=7),
+    dict(storage=3),
+])
+def test_validate_rejects_malformed(native_lib, bad):
+    from fuzzyblue_gb300 import _native as N
+    c = Parameters(**bad).to_c()
+    assert native_lib.fb_params_validate(ctypes.byref(c)) == N.FB_ERR_INVALID_PARAMS
+    assert native_lib.fb_last_error()
+
+
+def test_validate_accepts_benchmark_classes(native_lib):
+    for p in (Parameters(), smoke_parameters(),
+              Parameters(transmittance_mu_size=512, transmittance_r_size=128, irradiance_mu_s_size=128,
+                         irradiance_r_size=32, scattering_r_size=64, scattering_mu_size=256,
+                         scattering_mu_s_size=64, scattering_nu_size=16, order=8, transmittance_steps=2000),
+              Parameters(transmittance_mu_size=128, transmittance_r_size=32, scattering_r_size=16,
+                         scattering_mu_size=64, scattering_mu_s_size=16, scattering_nu_size=4)):
+        c = p.to_c()
+        assert native_lib.fb_params_validate(ctypes.byref(c)) == 0, native_lib.fb_last_error()
+
+
+def test_status_strings(native_lib):
+    assert native_lib.fb_status_string(0) == b"ok"
+    assert native_lib.fb_abi_version() == 1

@@ -1,0 +1,149 @@
+"""The CPU oracle against the golden vectors and against the reference's own
+shader code compiled as C++ (oracle/_ref), plus known-answer tests."""
+import os
+
+import numpy as np
+import pytest
+
+from fuzzyblue_gb300.params import (DensityProfile, DensityProfileLayer, Parameters, smoke_parameters)
+from tests.golden.make_golden import tiny_parameters
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def _params_from_record(rec):
+    from fuzzyblue_gb300.params import c_params
+    return bytes(np.asarray(rec, np.uint8))
+
+
+@pytest.mark.parametrize("name,mk", [("smoke_f32", smoke_parameters), ("tiny_f32", tiny_parameters)])
+def test_oracle_matches_golden_bitwise(oracle, name, mk):
+    g = np.load(os.path.join(GOLDEN, name + ".npz"))
+    p = mk()
+    assert bytes(p.to_c()) == _params_from_record(g["params"])
+    out = oracle.precompute(p, intermediates=True)
+    for k in ("transmittance", "irradiance", "scattering", "orders_ms", "orders_irr", "single_rayleigh", "single_mie"):
+        assert np.array_equal(out[k].view(np.uint32), g[k].view(np.uint32)), k
+
+
+def test_oracle_f16_storage_matches_golden(oracle):
+    g = np.load(os.path.join(GOLDEN, "smoke_f16.npz"))
+    out = oracle.precompute(smoke_parameters(storage=1))
+    for k in ("irradiance", "scattering"):
+        assert np.array_equal(out[k], g[k]), k
+
+
+def _random_atmosphere(seed):
+    rng = np.random.default_rng(seed)
+    R = float(rng.uniform(3000, 8000))
+    th = float(rng.uniform(40, 120))
+    hr, hm = float(rng.uniform(4, 12)), float(rng.uniform(0.5, 3))
+    f = float(np.exp(rng.uniform(np.log(0.2), np.log(5))))
+    mie = float(np.exp(rng.uniform(np.log(1e-3), np.log(5e-2))))
+    alb = float(rng.uniform(0.8, 1.0))
+    return Parameters(order=3, scattering_r_size=6, scattering_mu_size=12, scattering_mu_s_size=6,
+                      scattering_nu_size=3, transmittance_mu_size=40, transmittance_r_size=10,
+                      irradiance_mu_s_size=12, irradiance_r_size=5,
+                      bottom_radius=R, top_radius=R + th,
+                      rayleigh_scattering=tuple(f * c for c in (0.005802, 0.013558, 0.0331)),
+                      rayleigh_density=DensityProfile([DensityProfileLayer(), DensityProfileLayer(exp_term=1.0, exp_scale=-1 / hr)]),
+                      mie_scattering=(mie,) * 3, mie_extinction=(mie / alb,) * 3,
+                      mie_density=DensityProfile([DensityProfileLayer(), DensityProfileLayer(exp_term=1.0, exp_scale=-1 / hm)]),
+                      mie_phase_function_g=float(rng.uniform(0.6, 0.9)))
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_oracle_matches_reference_shaders(oracle, seed):
+    """Bitwise agreement with the reference's GLSL compiled as C++ on random
+    atmospheres (skipped where the reference checkout is not available)."""
+    if oracle.ref_lib() is None:
+        pytest.skip("reference shader build unavailable")
+    p = _random_atmosphere(seed)
+    a = oracle.precompute(p, intermediates=True)
+    b = oracle.precompute(p, intermediates=True, reference=True)
+    for k in a:
+        assert np.array_equal(a[k].view(np.uint32), b[k].view(np.uint32)), k
+
+
+def _zero_atmosphere(**kw):
+    z = (0.0, 0.0, 0.0)
+    return smoke_parameters(rayleigh_scattering=z, mie_scattering=z, mie_extinction=z, absorbtion_extinction=z, **kw)
+
+
+def test_kat_empty_atmosphere(oracle):
+    out = oracle.precompute(_zero_atmosphere(), np.float64)
+    assert np.all(out["transmittance"][..., :3] == 1.0)
+    assert np.all(out["scattering"] == 0.0)
+    assert np.all(out["irradiance"] == 0.0)
+
+
+def test_kat_constant_density_transmittance(oracle):
+    """Constant density 1 in every layer: T = exp(-beta * d_top) with d_top the
+    exact distance to the top boundary (the trapezoid rule is exact)."""
+    const = DensityProfile([DensityProfileLayer(constant_term=1.0), DensityProfileLayer(constant_term=1.0)])
+    zero = DensityProfile([DensityProfileLayer(), DensityProfileLayer()])
+    beta = (0.01, 0.02, 0.03)
+    p = smoke_parameters(rayleigh_scattering=beta, rayleigh_density=const, mie_density=zero,
+                         absorbtion_density=zero, mie_extinction=(0, 0, 0), mie_scattering=(0, 0, 0),
+                         absorbtion_extinction=(0, 0, 0), order=1)
+    tr = oracle.precompute(p, np.float64)["transmittance"]
+    R, T = p.bottom_radius, p.top_radius
+    H = np.sqrt(T * T - R * R)
+    nmu, nr = p.transmittance_extent()
+    for j in (0, 17, nr - 1):
+        for i in (0, 100, nmu - 1):
+            rho = H * j / (nr - 1)
+            r = np.sqrt(rho * rho + R * R)
+            dmin, dmax = T - r, rho + H
+            d = dmin + i / (nmu - 1) * (dmax - dmin)
+            assert np.allclose(tr[j, i, :3], np.exp(-np.array(beta) * d), rtol=1e-9)
+
+
+def test_kat_direct_irradiance(oracle):
+    """Direct irradiance = solar * T(r, mu_s) * mu_s for mu_s above the sun's
+    angular radius (direct_irradiance.comp:20-26)."""
+    p = smoke_parameters(order=1)
+    tr = oracle.precompute(p, np.float32)["transmittance"]
+    ir = oracle.direct_irradiance(p, tr)
+    nmus, nr = p.irradiance_extent()
+    ir = ir.reshape(nr, nmus, 4)
+    for j in range(nr):
+        for i in range(nmus):
+            mu_s = 2 * i / (nmus - 1) - 1
+            if mu_s > 0.05:
+                r = p.bottom_radius + j / (nr - 1) * (p.top_radius - p.bottom_radius)
+                assert np.all(ir[j, i, :3] > 0)
+                ratio = ir[j, i, :3] / (np.array(p.solar_irradiance) * mu_s)
+                assert np.all(ratio <= 1.0 + 1e-5) and np.all(ratio > 0)
+
+
+def test_kat_order_one(oracle):
+    """order = 1: irradiance stays cleared, scattering = single scattering."""
+    out = oracle.precompute(smoke_parameters(order=1), intermediates=True)
+    assert np.all(out["irradiance"] == 0)
+    sc, r, m = out["scattering"], out["single_rayleigh"], out["single_mie"]
+    assert np.array_equal(sc[..., :3], r[..., :3]) and np.array_equal(sc[..., 3], m[..., 0])
+
+
+def test_kat_phase_functions_integrate_to_one():
+    """The Rayleigh and Cornette-Shanks phase functions integrate to ~1 over the
+    16 x 32 direction grid of scattering_density.comp:34-66. The grid resolves
+    Rayleigh to 0.25%; the g = 0.8 forward peak of Mie only to ~5.4% (a
+    property of the reference's quadrature, not of this implementation)."""
+    n = 16
+    th = (np.arange(n) + 0.5) * np.pi / n
+    ph = (np.arange(2 * n) + 0.5) * np.pi / n
+    T, P = np.meshgrid(th, ph, indexing="ij")
+    dom = (np.pi / n) ** 2 * np.sin(T)
+    nu = np.cos(T)  # angle to the zenith axis
+    ray = 3 / (16 * np.pi) * (1 + nu * nu)
+    g = 0.8
+    mie = 3 / (8 * np.pi) * (1 - g * g) / (2 + g * g) * (1 + nu * nu) / (1 + g * g - 2 * g * nu) ** 1.5
+    assert abs((ray * dom).sum() - 1) < 3e-3
+    assert abs((mie * dom).sum() - 1) < 6e-2
+
+
+def test_oracle_rejects_invalid(oracle):
+    p = smoke_parameters().replace(scattering_mu_size=31)
+    with pytest.raises(RuntimeError):
+        oracle.precompute(p)

@@ -1,0 +1,176 @@
+"""GPU parity: the CUDA library (through the C ABI) against the golden vectors
+of the reference's shader code and against the CPU oracle.
+
+Tolerances (relative error with the floor 1e-6 * max|ref|, tests/errors.py):
+  PLAIN vs FP32 reference/oracle, whole precompute   max 2e-3, rms 1e-4
+  PLAIN vs FP32 oracle, one pass on the same inputs  max 2e-2, p99.9 2e-3
+      (same FP32 arithmetic; the differences come from expf/powf/sinf ulps and
+      summation order, amplified in a few ill-conditioned texels such as
+      twilight directions at the ground, where the FP32 reference itself is
+      1.5% away from the FP64 value)
+  MIXED vs FP64 oracle, whole precompute and each pass   max 1e-3 (the target)
+"""
+import os
+
+import numpy as np
+import pytest
+
+from fuzzyblue_gb300.params import (PRECISION_MIXED, Parameters, smoke_parameters)
+from tests.errors import rel_err, summary
+from tests.golden.make_golden import tiny_parameters
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+PLAIN_MAX, PLAIN_RMS = 2e-3, 1e-4
+PASS_MAX, PASS_P999 = 2e-2, 2e-3
+MIXED_MAX = 1e-3
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu_build(builder, p, intermediates=False):
+    from fuzzyblue_gb300.api import Atmosphere
+    pend = Atmosphere.build(builder, p)
+    pend.wait()
+    pend.assert_ready()
+    out = pend.atmosphere().to_host()
+    if intermediates:
+        out["_inter"] = {k: v.to_numpy() for k, v in pend.intermediates().items()}
+    pend.release()
+    return out
+
+
+def _check(out, ref, keys, max_tol, rms_tol=None):
+    for k in keys:
+        s = summary(out[k], ref[k])
+        assert np.isfinite(out[k]).all(), k
+        assert s["max"] <= max_tol, (k, s)
+        if rms_tol is not None:
+            assert s["rms"] <= rms_tol, (k, s)
+
+
+@pytest.mark.parametrize("name,mk", [("smoke_f32", smoke_parameters), ("tiny_f32", tiny_parameters)])
+def test_plain_matches_reference_golden(builder, name, mk):
+    g = np.load(os.path.join(GOLDEN, name + ".npz"))
+    out = gpu_build(builder, mk())
+    _check(out, g, ("transmittance", "irradiance", "scattering"), PLAIN_MAX, PLAIN_RMS)
+    # alpha channels: transmittance A = 1, irradiance A = 0, scattering A = single Mie red
+    assert np.all(out["transmittance"][..., 3] == 1.0)
+    assert np.all(out["irradiance"][..., 3] == 0.0)
+    a = rel_err(out["scattering"][..., 3:4].repeat(3, -1), g["scattering"][..., 3:4].repeat(3, -1))
+    assert a.max() <= PLAIN_MAX
+
+
+def test_plain_f16_storage_matches_reference_golden(builder):
+    g = np.load(os.path.join(GOLDEN, "smoke_f16.npz"))
+    out = gpu_build(builder, smoke_parameters(storage=1))
+    # both sides round to half on every store: allow one half ulp (4.9e-4) plus FP32 noise
+    _check(out, g, ("irradiance", "scattering"), 2e-3)
+
+
+def test_plain_per_order_matches_oracle(builder, oracle):
+    """Builds with order = 1..4: each final table against the oracle's."""
+    for order in (1, 2, 3, 4):
+        p = smoke_parameters(order=order)
+        ref = oracle.precompute(p)
+        out = gpu_build(builder, p)
+        _check(out, ref, ("transmittance", "irradiance", "scattering"), PLAIN_MAX, PLAIN_RMS)
+
+
+def test_mixed_meets_fp64_target(builder, oracle):
+    for p in (smoke_parameters(precision=PRECISION_MIXED), tiny_parameters().replace(precision=PRECISION_MIXED)):
+        ref = oracle.precompute(p, np.float64)
+        out = gpu_build(builder, p)
+        _check(out, ref, ("transmittance", "irradiance", "scattering"), MIXED_MAX)
+
+
+def _subset(rng, n, k):
+    return np.sort(rng.choice(n, size=min(n, k), replace=False))
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_each_pass_at_default_size(builder, oracle, precision):
+    """Parameters::default() sizes: every pass of the GPU against the oracle's
+    same pass on the GPU's own inputs, on a random subset of texels (PLAIN
+    against the FP32 oracle, MIXED against the FP64 oracle)."""
+    rng = np.random.default_rng(7)
+    base = Parameters(precision=precision)
+    dt = np.float64 if precision else np.float32
+    chk = (lambda r, g, w: _close64(r, g, w)) if precision else (lambda r, g, w: _close32(r, g, w))
+    p2 = base.replace(order=2)
+    o2 = gpu_build(builder, p2, intermediates=True)
+    it = o2["_inter"]
+    ntr, nir, nsc = p2.texel_counts()
+    tr = o2["transmittance"]
+    idx = _subset(rng, ntr, 512)
+    chk(oracle.transmittance(p2, idx, dtype=dt), tr.reshape(-1, 4)[idx], "transmittance")
+    idx = _subset(rng, nir, 256)
+    chk(oracle.direct_irradiance(p2, tr, idx, dtype=dt), it["delta_irradiance_0"].reshape(-1, 4)[idx], "direct")
+    idx = _subset(rng, nsc, 1024)
+    r, m = oracle.single_scattering(p2, tr, idx, dtype=dt)
+    chk(r, it["delta_rayleigh"].reshape(-1, 4)[idx], "single rayleigh")
+    chk(m, it["delta_mie"].reshape(-1, 4)[idx], "single mie")
+    idx = _subset(rng, nsc, 512)
+    d = oracle.scattering_density(p2, 2, tr, it["delta_rayleigh"], it["delta_mie"], None, it["delta_irradiance_0"],
+                                  idx, dtype=dt)
+    chk(d, it["scattering_density"].reshape(-1, 4)[idx], "density order 2")
+    idx = _subset(rng, nir, 128)
+    e = oracle.indirect_irradiance(p2, 1, it["delta_rayleigh"], it["delta_mie"], None, idx, dtype=dt)
+    chk(e, it["delta_irradiance_1"].reshape(-1, 4)[idx], "indirect order 1")
+    idx = _subset(rng, nsc, 1024)
+    ms, _ = oracle.multiple_scattering(p2, tr, it["scattering_density"], idx, dtype=dt)
+    chk(ms, it["delta_multiple_scattering"].reshape(-1, 4)[idx], "multiple order 2")
+    # order 3 density reads the order-2 multiple scattering and the order-1 irradiance
+    o3 = gpu_build(builder, base.replace(order=3), intermediates=True)
+    idx = _subset(rng, nsc, 512)
+    d3 = oracle.scattering_density(p2, 3, tr, None, None, it["delta_multiple_scattering"],
+                                   it["delta_irradiance_1"], idx, dtype=dt)
+    chk(d3, o3["_inter"]["scattering_density"].reshape(-1, 4)[idx], "density order 3")
+    idx = _subset(rng, nir, 128)
+    e2 = oracle.indirect_irradiance(p2, 2, None, None, it["delta_multiple_scattering"], idx, dtype=dt)
+    chk(e2, o3["_inter"]["delta_irradiance_0"].reshape(-1, 4)[idx], "indirect order 2")
+
+
+def _close32(ref, got, what):
+    s = summary(got, ref)
+    assert np.isfinite(got).all(), what
+    assert s["max"] <= PASS_MAX and s["p999"] <= PASS_P999, (what, s)
+
+
+def _close64(ref, got, what):
+    s = summary(got, ref)
+    assert np.isfinite(got).all(), what
+    assert s["max"] <= MIXED_MAX, (what, s)
+
+
+def test_batch_equals_single_builds(builder):
+    """A batch with mixed table classes, orders and precision modes gives the
+    same tables as building each atmosphere alone."""
+    from fuzzyblue_gb300.api import build_batch
+    ps = [smoke_parameters(), tiny_parameters(), smoke_parameters(order=2, precision=PRECISION_MIXED),
+          tiny_parameters().replace(order=5), smoke_parameters(storage=1)]
+    pend = build_batch(builder, ps)
+    pend.wait()
+    outs = [pend.atmosphere(i).to_host() for i in range(len(ps))]
+    pend.release()
+    for p, o in zip(ps, outs):
+        s = gpu_build(builder, p)
+        for k in ("transmittance", "irradiance", "scattering"):
+            assert np.array_equal(o[k], s[k]), k
+
+
+def test_zero_atmosphere(builder):
+    z = (0.0, 0.0, 0.0)
+    p = smoke_parameters(rayleigh_scattering=z, mie_scattering=z, mie_extinction=z, absorbtion_extinction=z)
+    for prec in (0, 1):
+        out = gpu_build(builder, p.replace(precision=prec))
+        assert np.all(out["transmittance"][..., :3] == 1.0)
+        assert np.all(out["scattering"] == 0.0)
+        assert np.all(out["irradiance"] == 0.0)
+
+
+def test_invalid_parameters_rejected_before_launch(builder):
+    from fuzzyblue_gb300 import _native as N
+    from fuzzyblue_gb300.api import Atmosphere
+    with pytest.raises(N.FuzzyblueError) as ei:
+        Atmosphere.build(builder, smoke_parameters().replace(scattering_mu_size=33))
+    assert ei.value.status == N.FB_ERR_INVALID_PARAMS
