@@ -1,0 +1,391 @@
+#!/usr/bin/env python3
+"""Benchmark: batched atmosphere LUT precompute on GB300.
+
+Headline workload (one "step"): a batch of 256 seeded synthetic atmospheres
+(fuzzyblue_gb300.workloads.uniform_batch, seed 0) at the crate's default table
+sizes (transmittance 256x64, irradiance 64x16, scattering r32 mu128 mu_s32 nu8),
+4 scattering orders, MIXED precision (max relative error <= 1e-3 against the
+FP64 oracle), built with one persistent launch per pass group.
+
+  value   atmospheres/s with the work resident on the device (CUDA events on the
+          build stream; per-launch events give the kernel times)
+  e2e     atmospheres/s through the public API: parameters from the host, every
+          table of every atmosphere copied back into pinned host memory
+  plain   the plain path, one default atmosphere per call, FP32 (for the
+          batched/plain ratio)
+  cpu_baseline  the reference's own shader code compiled as C++ (oracle/_ref), or
+          the oracle port where that is unavailable, on a bounded sample, all
+          host threads
+
+--impl reference times the reference's CPU implementation on the same metric.
+Multi-GPU: replicas only (each rank builds its own batch; no collective on the
+data path); value is the whole-job rate.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+BATCH = 256
+ORDERS = 4
+WORKLOAD = ("uniform batch: 256 seeded atmospheres (seed 0), default table sizes "
+            "(TR 256x64, IR 64x16, SC r32 mu128 mu_s32 nu8), 4 orders, mixed precision")
+METRIC = "atmospheres/s, uniform batch of 256 at default table sizes, 4 orders, mixed precision (<=1e-3 rel err vs FP64)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--batch", type=int, default=BATCH)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ clocks --
+class Clocks:
+    """Samples nvidia-smi every 200 ms while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                rows.append(f)
+        os.unlink(self.path)
+        if not rows:
+            return None
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in rows if num(r[2]) is not None]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for n, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+# ------------------------------------------------------------ distributed --
+def dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as td
+        td.barrier()
+
+
+def max_over_ranks(world, v):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as td
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    td.all_reduce(t, op=td.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------- roofline ---
+# Work of the dominant kernel (scattering density + indirect irradiance): the
+# unit is one direction evaluation of the scattering-density integrand
+# (scattering_density.comp:62-104), 2 * density_samples^2 directions per texel,
+# plus 16 x 64 per irradiance texel. FLOPs per direction evaluation of the
+# kernel's algorithm (order >= 3, counted in fb_passes.cuh tile_density's inner
+# loop: FP32 adds, multiplies and FMAs as 2, MUFU ops as 1).
+FLOP_PER_DIRECTION = 46.0
+
+
+def fp32_peak_tflops(sms, mhz):
+    return sms * 128 * 2 * mhz * 1e6 / 1e12
+
+
+def read_traffic():
+    path = os.path.join(ROOT, "profiles", "density_default_mixed_ncu.txt")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_launch_order3:"):
+                return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return {}
+
+
+# ------------------------------------------------------------------ ours ---
+def run_ours(a):
+    world, rank, local = dist()
+    import numpy as np
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as td
+        td.init_process_group("nccl")
+    from fuzzyblue_gb300 import workloads
+    from fuzzyblue_gb300.api import Atmosphere, Builder, build_batch
+    from fuzzyblue_gb300.params import Parameters
+
+    builder = Builder(local)
+    stream = torch.cuda.Stream()
+    params = workloads.uniform_batch(a.batch, seed=0, order=ORDERS)
+
+    def step(profile=False):
+        builder.set_profiling(profile)
+        pend = build_batch(builder, params, stream=stream)
+        return pend
+
+    # warm-up (graph path)
+    for _ in range(a.warmup):
+        p = step()
+        p.wait()
+        p.release()
+    torch.cuda.synchronize()
+
+    # timed region: device-resident work, per-launch timing events
+    clocks = Clocks(local)
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    step_ms, prof = [], []
+    ev0.record(stream)
+    for _ in range(a.steps):
+        s0 = torch.cuda.Event(enable_timing=True)
+        s1 = torch.cuda.Event(enable_timing=True)
+        s0.record(stream)
+        p = step(profile=True)
+        s1.record(stream)
+        p.wait()
+        prof.append(p.profile())
+        p.release()
+        step_ms.append(s0.elapsed_time(s1))
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    total_ms = max_over_ranks(world, ev0.elapsed_time(ev1))
+    ms_per_step = total_ms / a.steps
+    value = world * a.batch / (ms_per_step / 1e3)
+
+    # the same steps replayed from the CUDA graph (no per-launch events)
+    builder.set_profiling(False)
+    torch.cuda.synchronize()
+    g0, g1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    g0.record(stream)
+    for _ in range(a.steps):
+        p = step()
+        p.wait()
+        p.release()
+    g1.record(stream)
+    torch.cuda.synchronize()
+    graph_ms = max_over_ranks(world, g0.elapsed_time(g1)) / a.steps
+
+    # end to end through the public API with host buffers
+    sizes = params[0].texel_counts()
+    per_atm = 16 * sum(sizes)
+    host = torch.empty((a.batch, per_atm // 4), dtype=torch.float32, pin_memory=True).numpy()
+    tw, th = params[0].transmittance_extent()
+    iw, ih = params[0].irradiance_extent()
+    n_tr, n_ir = 4 * tw * th, 4 * iw * ih
+    import ctypes
+    from fuzzyblue_gb300 import _native as N
+    h2d = a.batch * 384
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        p = build_batch(builder, params, stream=stream)
+        p.wait()
+        for i in range(a.batch):
+            base = host[i].ctypes.data
+            atm = p.atmosphere(i)
+            N.check(N.lib().fb_atmosphere_copy_to_host(atm._h, stream.cuda_stream, base, base + 4 * n_tr,
+                                                       base + 4 * (n_tr + n_ir)), "copy_to_host")
+        p.release()
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(world, time.perf_counter() - t0) / a.steps
+    e2e = world * a.batch / e2e_s
+
+    # plain path: one default-size atmosphere per call, FP32
+    plain_p = Parameters()
+    for _ in range(2):
+        q = Atmosphere.build(builder, plain_p, stream=stream)
+        q.wait()
+        q.release()
+    pe0, pe1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n_plain = 20
+    pe0.record(stream)
+    for _ in range(n_plain):
+        q = Atmosphere.build(builder, plain_p, stream=stream)
+        q.release()
+    pe1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = pe0.elapsed_time(pe1) / n_plain
+
+    # kernel times from the timed region
+    kernels = {}
+    for launches in prof:
+        for r in launches:
+            key = r["kernel"] + ("" if r["order"] == 0 else "_order%d" % min(r["order"], 3))
+            kernels.setdefault(key, []).append(r)
+    dens = [r for launches in prof for r in launches if r["kernel"] == "density+indirect" and r["order"] >= 3]
+    dens_ms = sum(r["ms"] for r in dens) / max(len(dens), 1)
+    sms = builder.sm_count
+    dirs = 2 * params[0].density_samples ** 2
+    units = a.batch * (sizes[2] * dirs + sizes[1] * 16 * 64)
+    achieved = units * FLOP_PER_DIRECTION / (dens_ms / 1e3) / 1e12
+    mhz = (clk or {}).get("sm_mhz") or 2070.0
+    peak = fp32_peak_tflops(sms, mhz)
+    traffic = read_traffic()
+    peaks = measured_peaks()
+
+    out = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "atmospheres/s",
+        "n_gpus": world,
+        "steps": a.steps,
+        "warmup": a.warmup,
+        "ms_per_step": ms_per_step,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 with f64 ray geometry and order accumulation",
+        "data": "synthetic: seeded atmospheres (fuzzyblue_gb300.workloads, seed 0)",
+        "config": {"workload": WORKLOAD, "batch_per_gpu": a.batch, "orders": ORDERS, "precision": "mixed",
+                   "parallelism": "replicas" if world > 1 else "single",
+                   "l2": "inputs larger than L2: ~%d GB of tables and temporaries per step" % round(
+                       a.batch * 0.1)},
+        "clocks": clk,
+        "e2e": {"value": e2e, "unit": "atmospheres/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": a.batch * per_atm},
+        "gpu_launches": sum(len(x) for x in prof),
+        "roofline": {"bound": "fp32", "kernel": "k_density (scattering density + indirect irradiance), order >= 3",
+                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                     "peak_source": "152 SMs x 128 FP32 lanes x 2 FLOP x median SM clock under load (%d MHz); "
+                                    "the kernel uses neither HBM bandwidth nor tensor cores at their limits" % mhz,
+                     "launch_ms": dens_ms, "flop_per_direction": FLOP_PER_DIRECTION,
+                     "hbm": {"achieved_gbs": (traffic or 0) / (dens_ms / 1e3) / 1e9 if traffic else None,
+                             "peak_gbs": peaks.get("hbm_gbs"), "peak_source": "MEASURED_PEAKS.json"},
+                     "traffic": traffic},
+        "kernels_ms": {k: sum(r["ms"] for r in v) / len(v) for k, v in sorted(kernels.items())},
+        "latency_ms": {"p50": statistics.median(step_ms), "p99": float(np.quantile(step_ms, 0.99))},
+        "graph": {"ms_per_step": graph_ms, "value": world * a.batch / (graph_ms / 1e3)},
+        "plain": {"ms_per_atmosphere": plain_ms, "atmospheres_per_s": 1e3 / plain_ms, "precision": "plain"},
+        "batched_over_plain": value / (world * 1e3 / plain_ms),
+    }
+    if rank == 0 and not a.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(params[0])
+    if rank == 0:
+        print(json.dumps(out))
+    builder.close()
+    if world > 1:
+        import torch.distributed as td
+        td.destroy_process_group()
+
+
+def cpu_baseline(p, fraction=1.0 / 8):
+    from oracle import cpu_baseline as C
+    kind = "reference" if C.reference_available() else "port"
+    r = C.estimate(p, "reference" if kind == "reference" else "port", fraction=fraction)
+    return {"value": 1.0 / r["seconds_per_atmosphere"], "unit": "atmospheres/s", "cores": r["threads"],
+            "kind": kind, "sample": r["sample"], "sample_seconds": r["sample_seconds"]}
+
+
+# ------------------------------------------------------------- reference ---
+def run_reference(a):
+    world, rank, local = dist()
+    if rank != 0:
+        return
+    from fuzzyblue_gb300 import workloads
+    from oracle import cpu_baseline as C
+    kind = "reference" if C.reference_available() else "port"
+    p = workloads.uniform_batch(1, seed=0, order=ORDERS)[0]
+    frac = 1.0 / 32
+    for _ in range(a.warmup):
+        C.estimate(p, kind, fraction=frac)
+    t0 = time.perf_counter()
+    est = []
+    for _ in range(a.steps):
+        est.append(C.estimate(p, kind, fraction=frac))
+    wall = time.perf_counter() - t0
+    sec = statistics.mean(r["seconds_per_atmosphere"] for r in est)
+    value = 1.0 / sec
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "atmospheres/s", "n_gpus": world,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": wall / a.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: seeded atmospheres (fuzzyblue_gb300.workloads, seed 0)",
+        "config": {"workload": WORKLOAD, "batch_per_gpu": a.batch, "orders": ORDERS, "precision": "reference FP32",
+                   "implementation": "the reference's shaders compiled as C++ (oracle/_ref), host threads"
+                   if kind == "reference" else "the oracle's C++ restatement (oracle/fb_oracle.cpp), host threads"},
+        "cpu_baseline": {"value": value, "unit": "atmospheres/s", "cores": est[0]["threads"], "kind": kind,
+                         "sample": est[0]["sample"]},
+        "e2e": {"value": value, "unit": "atmospheres/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)
+
+
+if __name__ == "__main__":
+    main()

@@ -18,7 +18,7 @@ __all__ = [
 def __getattr__(name):
     # The API objects need the native library; import them lazily so that
     # parameter handling works without it.
-    if name in ("Atmosphere", "Builder", "PendingAtmosphere", "build_batch", "DeviceArray", "validate",
+    if name in ("Atmosphere", "Builder", "PendingAtmosphere", "Server", "build_batch", "DeviceArray", "validate",
                 "device_bytes"):
         from . import api
         return getattr(api, name)

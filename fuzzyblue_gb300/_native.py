@@ -56,9 +56,10 @@ class c_server_config(ctypes.Structure):
     _fields_ = [
         ("hbm_budget_bytes", ctypes.c_uint64),
         ("max_batch", ctypes.c_uint32),
-        ("max_inflight_batches", ctypes.c_uint32),
+        ("max_inflight", ctypes.c_uint32),
         ("cache_entries", ctypes.c_uint32),
-        ("reserved", ctypes.c_uint32 * 7),
+        ("max_queue", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32 * 6),
     ]
 
 
@@ -76,6 +77,7 @@ class c_server_stats(ctypes.Structure):
         ("queued", ctypes.c_uint64),
         ("p50_ms", ctypes.c_double),
         ("p99_ms", ctypes.c_double),
+        ("mean_ms", ctypes.c_double),
         ("mean_batch", ctypes.c_double),
     ]
 
@@ -131,6 +133,15 @@ SIGNATURES = {
     "fb_atmosphere_destroy": (None, [_V]),
     "fb_batch_build": (_I, [_V, _V, _P, _U32, ctypes.POINTER(_V)]),
     "fb_builder_set_profiling": (_I, [_V, _I]),
+    "fb_server_config_default": (None, [ctypes.POINTER(c_server_config)]),
+    "fb_server_create": (_I, [_V, ctypes.POINTER(c_server_config), ctypes.POINTER(_V)]),
+    "fb_server_submit": (_I, [_V, _P, ctypes.POINTER(_U64)]),
+    "fb_server_poll": (_I, [_V, _U64, ctypes.POINTER(_V)]),
+    "fb_server_wait": (_I, [_V, _U64, _U32, ctypes.POINTER(_V)]),
+    "fb_server_release": (_I, [_V, _U64]),
+    "fb_server_cancel": (_I, [_V, _U64]),
+    "fb_server_get_stats": (_I, [_V, ctypes.POINTER(c_server_stats)]),
+    "fb_server_destroy": (None, [_V]),
     "fb_pending_profile": (_I, [_V, ctypes.POINTER(c_launch_profile), _U32, ctypes.POINTER(_U32)]),
     "fb_status_string": (ctypes.c_char_p, [_I]),
     "fb_last_error": (ctypes.c_char_p, []),

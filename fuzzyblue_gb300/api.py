@@ -287,3 +287,73 @@ def device_bytes(params: Parameters):
     t = ctypes.c_uint64()
     N.check(N.lib().fb_params_device_bytes(ctypes.byref(c), ctypes.byref(o), ctypes.byref(t)), "device_bytes")
     return o.value, t.value
+
+
+class Server:
+    """Request loop with HBM-budget admission, concurrent batches and a
+    device-resident LRU cache of finished tables (fb_server_* in the C ABI)."""
+
+    def __init__(self, builder: Builder, hbm_budget_bytes: Optional[int] = None, max_batch: Optional[int] = None,
+                 max_inflight: Optional[int] = None, cache_entries: Optional[int] = None,
+                 max_queue: Optional[int] = None):
+        cfg = N.c_server_config()
+        N.lib().fb_server_config_default(ctypes.byref(cfg))
+        for name, v in (("hbm_budget_bytes", hbm_budget_bytes), ("max_batch", max_batch),
+                        ("max_inflight", max_inflight), ("cache_entries", cache_entries), ("max_queue", max_queue)):
+            if v is not None:
+                setattr(cfg, name, v)
+        self.config = cfg
+        self._h = ctypes.c_void_p()
+        N.check(N.lib().fb_server_create(builder.handle, ctypes.byref(cfg), ctypes.byref(self._h)), "fb_server_create")
+        self._builder = builder
+        self._params: Dict[int, Parameters] = {}
+
+    def submit(self, params: Parameters) -> int:
+        t = ctypes.c_uint64()
+        c = params.to_c()
+        N.check(N.lib().fb_server_submit(self._h, ctypes.byref(c), ctypes.byref(t)), "fb_server_submit")
+        self._params[t.value] = params
+        return t.value
+
+    def _atm(self, ticket, h):
+        return Atmosphere(h, self._params[ticket], owned=False, keepalive=self)
+
+    def poll(self, ticket: int) -> Optional[Atmosphere]:
+        h = ctypes.c_void_p()
+        rc = N.check(N.lib().fb_server_poll(self._h, ticket, ctypes.byref(h)), "fb_server_poll")
+        return None if rc == N.FB_NOT_READY else self._atm(ticket, h)
+
+    def wait(self, ticket: int, timeout_ms: int = 0xFFFFFFFF) -> Optional[Atmosphere]:
+        h = ctypes.c_void_p()
+        rc = N.check(N.lib().fb_server_wait(self._h, ticket, timeout_ms, ctypes.byref(h)), "fb_server_wait")
+        return None if rc == N.FB_NOT_READY else self._atm(ticket, h)
+
+    def release(self, ticket: int):
+        N.check(N.lib().fb_server_release(self._h, ticket), "fb_server_release")
+        self._params.pop(ticket, None)
+
+    def cancel(self, ticket: int) -> bool:
+        """True if the request was cancelled before it started."""
+        return N.check(N.lib().fb_server_cancel(self._h, ticket), "fb_server_cancel") == N.FB_OK
+
+    def stats(self) -> dict:
+        s = N.c_server_stats()
+        N.check(N.lib().fb_server_get_stats(self._h, ctypes.byref(s)), "fb_server_get_stats")
+        return {name: getattr(s, name) for name, _ in N.c_server_stats._fields_}
+
+    def close(self):
+        if self._h:
+            N.lib().fb_server_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

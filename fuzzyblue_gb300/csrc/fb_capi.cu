@@ -507,9 +507,9 @@ void plan_group(Plan& P, const std::vector<DevAtmo>& A, const std::vector<int>& 
     std::vector<int> t0, t1;
     for (int j : jobs) {
       const DevAtmo& a = A[j];
-      t0.push_back(fb::tiles_density(a.sc_r, a.sc_mus, a.sc_mu, a.dens_chunk));
+      t0.push_back(fb::tiles_density(a));
       t1.push_back(fb::tiles_indirect(a.ir_mus, a.ir_r));
-      D.smem = std::max(D.smem, fb::density_smem(a.dens_n, a.sc_nu, a.ir_mus, a.dens_chunk, n == 2));
+      D.smem = std::max(D.smem, fb::density_smem(a, n == 2, mixed));
       D.smem = std::max(D.smem, fb::indirect_smem(a.irr_n, a.sc_nu, n - 1 == 1));
       D.texels += (uint64_t)a.W * a.sc_mu * a.sc_r + (uint64_t)a.ir_mus * a.ir_r;
     }
@@ -571,7 +571,7 @@ void fill_devatmo(DevAtmo& d, const fb_params& p, const fbi::Tuning& tun) {
   d.order = (int)p.order;
   d.f16 = p.storage == FB_STORAGE_F16;
   d.W = d.sc_nu * d.sc_mus;
-  d.dens_chunk = fbi::tuning_density_chunk(tun, d.sc_r, d.sc_mu, d.sc_mus, d.sc_nu);
+  fbi::tuning_density_shape(tun, d.sc_r, d.sc_mu, d.sc_mus, d.sc_nu, &d.dens_S, &d.dens_chunk);
 }
 
 }  // namespace
@@ -675,6 +675,7 @@ int build(fb_builder* b, cudaStream_t s, const fb_params* params, uint32_t count
     const void* fn;
     LaunchArgs args;
     int grid;
+    int block;
     size_t smem;
     fb_launch_profile info;
   };
@@ -702,7 +703,8 @@ int build(fb_builder* b, cudaStream_t s, const fb_params* params, uint32_t count
       total += L.seg_total[sidx];
     }
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, R.fn, fb::kThreads, R.smem) != cudaSuccess || per_sm < 1)
+    R.block = L.pass == fb::kPassDensity ? fb::kDensThreads : fb::kThreads;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, R.fn, R.block, R.smem) != cudaSuccess || per_sm < 1)
       return bail(FB_ERR_CUDA, "occupancy query failed");
     R.grid = std::max(1, std::min(total, per_sm * b->sms));
     std::memset(&R.info, 0, sizeof(R.info));
@@ -730,7 +732,7 @@ int build(fb_builder* b, cudaStream_t s, const fb_params* params, uint32_t count
     if (e == cudaSuccess && profiling) e = cudaEventRecord(P->marks[0], st);
     for (size_t k = 0; e == cudaSuccess && k < ready.size(); ++k) {
       void* args[] = {(void*)&ready[k].args};
-      e = cudaLaunchKernel(ready[k].fn, dim3(ready[k].grid), dim3(fb::kThreads), args, ready[k].smem, st);
+      e = cudaLaunchKernel(ready[k].fn, dim3(ready[k].grid), dim3(ready[k].block), args, ready[k].smem, st);
       if (e == cudaSuccess && profiling) e = cudaEventRecord(P->marks[k + 1], st);
     }
     return e;
@@ -765,6 +767,15 @@ int build(fb_builder* b, cudaStream_t s, const fb_params* params, uint32_t count
   *out = P;
   return FB_OK;
 }
+
+fb_atmosphere* pending_detach(fb_pending* p, uint32_t i) {
+  if (!p || i >= p->atms.size()) return nullptr;
+  fb_atmosphere* a = p->atms[i];
+  p->atms[i] = nullptr;
+  return a;
+}
+cudaEvent_t pending_event(fb_pending* p) { return p->done; }
+size_t atmosphere_bytes(const fb_atmosphere* a) { return sizes_of(a->params).out_bytes; }
 
 }  // namespace fbi
 

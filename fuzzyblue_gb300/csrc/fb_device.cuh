@@ -33,7 +33,7 @@ struct DevAtmo {
   int tr_steps, ss_steps, ms_steps, dens_n, irr_n, order;
   int f16;         // round the scattering-class tables to half on store
   int W;           // sc_nu * sc_mus, width of the packed 3D scattering tables
-  int dens_chunk;  // mu rows per scattering-density tile (autotuned per table class)
+  int dens_S, dens_chunk;  // scattering-density tile shape (0 = default; set by the autotuner)
   // outputs
   float4* tr;
   float4* ir;
@@ -404,9 +404,38 @@ struct MuS32 {
   __device__ __forceinline__ float texel(float mu_s) const {
     float s = R * mu_s;
     float root = sqrtf(fmaf(s, s, H2));
-    float d = s > 0.0f ? H2 / (s + root) : root - s;
+    float d = s > 0.0f ? __fdividef(H2, s + root) : root - s;
     float aa = (d - dmin) * inv_span;
-    return gmax(1.0f - aa * inv_A, 0.0f) / (1.0f + aa) * scale;
+    return __fdividef(gmax(1.0f - aa * inv_A, 0.0f), 1.0f + aa) * scale;
+  }
+};
+
+// PLAIN form of the mu_s texture coordinate (scattering.h:48-56), the
+// reference's float arithmetic with its per-atmosphere constants hoisted: the
+// divisions by constants become products with reciprocals (last-bit
+// differences only).
+struct MuSRef32 {
+  float R, RR, TT, dmin, inv_span, inv_A, c0, c1;
+  __device__ __forceinline__ void init(const DevAtmo& a) {
+    R = a.bottom;
+    RR = R * R;
+    const float T = a.top;
+    TT = T * T;
+    const float H = sqrtf(T * T - R * R);
+    dmin = T - R;
+    const float span = H - dmin;
+    inv_span = 1.0f / span;
+    const float A = -2.0f * a.mu_s_min * R / span;
+    inv_A = 1.0f / A;
+    c0 = 0.5f / float(a.sc_mus);
+    c1 = 1.0f - 1.0f / float(a.sc_mus);
+  }
+  // the texture coordinate u_mu_s
+  __device__ __forceinline__ float coord(float mu_s) const {
+    float disc = RR * (mu_s * mu_s - 1.0f) + TT;
+    float d = gmax(-R * mu_s + safe_sqrt(disc), 0.0f);
+    float aa = (d - dmin) * inv_span;
+    return c0 + gmax(1.0f - aa * inv_A, 0.0f) / (1.0f + aa) * c1;
   }
 };
 

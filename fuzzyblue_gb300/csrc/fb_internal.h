@@ -20,14 +20,14 @@ TableSizes sizes_of(const fb_params& p);
 // (fb_builder_autotune) or by the default rule.
 struct TuneEntry {
   int sc_r, sc_mu, sc_mus, sc_nu;
-  int density_chunk;
+  int dens_S, dens_chunk;  // scattering-density tile: mu_s columns x mu rows
 };
 struct Tuning {
   std::vector<TuneEntry> entries;
 };
 void tuning_load_default(Tuning& t);
-int tuning_density_chunk(const Tuning& t, int sc_r, int sc_mu, int sc_mus, int sc_nu);
-int default_density_chunk(int sc_mu, int sc_nu);
+// Tile shape of a table class (0, 0 when the class is not tuned: default rule).
+void tuning_density_shape(const Tuning& t, int sc_r, int sc_mu, int sc_mus, int sc_nu, int* S, int* chunk);
 
 void builder_ref(fb_builder* b);
 void builder_unref(fb_builder* b);
@@ -48,6 +48,10 @@ void atmosphere_tables(const fb_atmosphere* a, float4** tr, float4** ir, float4*
 
 int build(fb_builder* b, cudaStream_t s, const fb_params* params, uint32_t count, bool use_graph, fb_pending** out);
 void pending_destroy(fb_pending* p);
+// Removes atmosphere `index` from the pending handle (ownership to the caller).
+fb_atmosphere* pending_detach(fb_pending* p, uint32_t index);
+cudaEvent_t pending_event(fb_pending* p);
+size_t atmosphere_bytes(const fb_atmosphere* a);
 
 cudaError_t launch_to_half(const float4* src, void* dst, size_t n, cudaStream_t s);
 

@@ -297,7 +297,7 @@ __device__ __forceinline__ void texel_mus_nu(const DevAtmo& a, const RowInfo& ri
 
 // ============================================================ S: single ===
 struct SSRec {
-  float d, r_d, rr_d, dmin, span, tvx, tvy, tvz, rho_r, rho_m, w, cos_h, lo, hi, fy, e;
+  float d, r_d, inv_r, rr_d, dmin, inv_span, tvx, tvy, tvz, rho_r, rho_m, w, cos_h, lo, inv_w, fy, e;
   int y0, y1;
 };
 
@@ -345,10 +345,11 @@ __device__ void tile_single(const DevAtmo& a, int tile, unsigned char* smem) {
       float sin_h = G.R / r_d;
       o.cos_h = -sqrtf(gmax(1.0f - sin_h * sin_h, 0.0f));
       o.lo = -sin_h * a.sun_radius;
-      o.hi = sin_h * a.sun_radius;
+      o.inv_w = 1.0f / (sin_h * a.sun_radius - o.lo);
+      o.inv_r = 1.0f / r_d;
       float rho = safe_sqrt(r_d * r_d - G.R * G.R);
       o.dmin = G.T - r_d;
-      o.span = (rho + G.H) - o.dmin;
+      o.inv_span = 1.0f / ((rho + G.H) - o.dmin);
       v = coord_from_unit(rho / G.H, a.tr_r);
       o.e = 0.f;
       const Axis ay = make_axis(v, a.tr_r);
@@ -373,11 +374,12 @@ __device__ void tile_single(const DevAtmo& a, int tile, unsigned char* smem) {
       o.cos_h = (float)(-rho / r_d);
       double sin_h = G.R / r_d;
       o.lo = (float)(-sin_h * a.sun_radius);
-      o.hi = (float)(sin_h * a.sun_radius);
+      o.inv_w = (float)(1.0 / (2.0 * sin_h * a.sun_radius));
+      o.inv_r = (float)(1.0 / r_d);
       o.e = (float)(G.H2 - q);  // T^2 - r_d^2
       const double dmin = (G.H2 - q) / (G.T + r_d);
       o.dmin = (float)dmin;
-      o.span = (float)(rho + G.H - dmin);
+      o.inv_span = (float)(1.0 / (rho + G.H - dmin));
       const Axis ay = axis_texel(rho / G.H * double(a.tr_r - 1), a.tr_r);
       o.y0 = ay.i0;
       o.y1 = ay.i1;
@@ -389,6 +391,7 @@ __device__ void tile_single(const DevAtmo& a, int tile, unsigned char* smem) {
   }
   __syncthreads();
   const float TT = a.top * a.top;
+  const float trc0 = 0.5f / float(a.tr_mu), trc1 = 1.0f - 1.0f / float(a.tr_mu), trn = float(a.tr_mu);
   for (int k = tid; k < nrow * W; k += kThreads) {
     const int lr = k / W, x = k % W;
     const RowInfo& ri = rows[lr];
@@ -403,22 +406,24 @@ __device__ void tile_single(const DevAtmo& a, int tile, unsigned char* smem) {
       float x_mu, mu_s_d;
       if (!MX) {
         // single_scattering.comp:17, transmittance.h:63-74
-        mu_s_d = clamp_cosine((r_mu_s + o.d * nu) / o.r_d);
+        mu_s_d = clamp_cosine((r_mu_s + o.d * nu) * o.inv_r);
         float disc = o.rr_d * (mu_s_d * mu_s_d - 1.0f) + TT;
         float dt = gmax(-o.r_d * mu_s_d + safe_sqrt(disc), 0.0f);
-        x_mu = (dt - o.dmin) / o.span;
+        x_mu = (dt - o.dmin) * o.inv_span;
       } else {
         // distance to the top from (r_d, mu_s_d): T^2 - r_d^2 + (r_d mu_s_d)^2
         // under the root, rationalised when the ray points up.
         float s_d = gclamp(fmaf(o.d, nu, r_mu_s), -o.r_d, o.r_d);
-        mu_s_d = s_d / o.r_d;
+        mu_s_d = s_d * o.inv_r;
         float root = sqrtf(fmaf(s_d, s_d, o.e));
-        float dt = s_d > 0.0f ? o.e / (s_d + root) : root - s_d;
-        x_mu = (dt - o.dmin) / o.span;
+        float dt = s_d > 0.0f ? __fdividef(o.e, s_d + root) : root - s_d;
+        x_mu = (dt - o.dmin) * o.inv_span;
       }
-      const float sfac = smoothstepf(o.lo, o.hi, mu_s_d - o.cos_h);
+      // smoothstep(-sin_h alpha, sin_h alpha, mu_s_d - cos_h)
+      const float st = gclamp((mu_s_d - o.cos_h - o.lo) * o.inv_w, 0.0f, 1.0f);
+      const float sfac = st * st * (3.0f - 2.0f * st);
       const Axis ax = MX ? axis_texel(x_mu * float(a.tr_mu - 1), a.tr_mu)
-                         : make_axis(coord_from_unit(x_mu, a.tr_mu), a.tr_mu);
+                         : axis_texel(fmaf(fmaf(x_mu, trc1, trc0), trn, -0.5f), a.tr_mu);
       Axis ay;
       ay.i0 = o.y0;
       ay.i1 = o.y1;
@@ -461,334 +466,437 @@ template <bool MX> __global__ void __launch_bounds__(kThreads) k_single(LaunchAr
 }
 
 // ============================================================ density ===
-// scattering_density.comp:10-155 for a tile of texels sharing (r, mu_s): all
-// 4D lookups of the tile hit the previous order's table at the tile's r and
-// mu_s and at one of the 16 theta rows, so the table is first reduced by
-// trilinear interpolation to P[theta][nu slice]; each of the 512 directions of
-// a texel is then a linear blend of two P entries.
+// scattering_density.comp:10-155. A tile is a set of texels that share r (one
+// z slice) and S mu_s columns; each thread owns a "nu group": G texels that
+// share r, mu and mu_s and differ only in nu.
+//  * The previous order's table is looked up at the tile's r and mu_s and at
+//    one of the 16 theta rows only, so it is reduced once per tile by
+//    trilinear interpolation to P[column][theta][nu slice] (stored with the
+//    difference to the next slice): each 4D lookup becomes one linear blend.
+//  * The phase functions of the scattering angle omega . omega_i depend on mu
+//    and the direction only: they are evaluated once per thread and direction
+//    for all G texels.
+//  * Directions come in mirror pairs (phi, 2 pi - phi): same cos phi, opposite
+//    sin phi, hence the same angle to the view direction (omega has no y
+//    component), so each pair shares one phase evaluation.
+constexpr int kDensThreads = 128;
+constexpr int kDensMaxGroup = 8;
+
 struct DensTheta {
   float cos_t, domega, dg, tgx, tgy, tgz;
   int ground, pad;
 };
 
+// Per-atmosphere tile shape of the density pass (host and device agree).
+struct DensShape {
+  int G;      // texels per thread (divides nu_size, <= kDensMaxGroup)
+  int NG;     // nu groups per mu row
+  int S;      // mu_s columns per tile
+  int chunk;  // mu rows per tile
+  int scols, ychunks, tiles;
+};
+// S_req / chunk_req: a tile shape chosen by the autotuner (0 = default rule:
+// one mu_s column and every mu row that fits in the block).
+__host__ __device__ inline DensShape dens_shape(int sc_r, int sc_mu, int sc_mus, int sc_nu, int S_req = 0,
+                                                int chunk_req = 0) {
+  DensShape d;
+  d.G = (sc_nu % 8 == 0) ? 8 : (sc_nu % 4 == 0) ? 4 : (sc_nu % 2 == 0) ? 2 : 1;
+  d.NG = sc_nu / d.G;
+  const int per_col = sc_mu * d.NG;
+  if (S_req > 0 && chunk_req > 0 && S_req * min(chunk_req, sc_mu) * d.NG <= kDensThreads) {
+    d.S = min(S_req, sc_mus);
+    d.chunk = min(chunk_req, sc_mu);
+  } else if (per_col >= kDensThreads) {
+    d.S = 1;
+    d.chunk = max(1, kDensThreads / d.NG);
+  } else {
+    d.S = max(1, min(sc_mus, kDensThreads / per_col));
+    d.chunk = sc_mu;
+  }
+  d.scols = (sc_mus + d.S - 1) / d.S;
+  d.ychunks = (sc_mu + d.chunk - 1) / d.chunk;
+  d.tiles = sc_r * d.scols * d.ychunks;
+  return d;
+}
+
 struct DensLayout {
-  DensTheta* th;
-  Axis* tay;    // theta -> mu axis
-  Axis* kax;    // nu slice -> x axis
-  float2* dir;  // (cos phi sin theta, sin phi sin theta) per direction
-  float4* gn;   // ground normal per direction (ground thetas)
-  float4* P;    // reduced table(s)
-  float4* irow; // two irradiance rows at the ground
-  double2* ymu;  // MIXED: per mu row (mu, 1 - mu^2)
-  double* nuraw; // MIXED: raw nu per nu index
+  DensTheta* th;    // NT
+  Axis* tay;        // NT: theta -> mu axis
+  Axis* kax;        // S * NK: (column, nu slice) -> x axis
+  float4* dir;      // NT * NT mirror pairs: (cos phi sin t, sin phi sin t, ground normal x, y)
+  float* gnz;       // NT * NT: ground normal z
+  float4* P;        // S * NT * NK * 2 float4 per table (value.rgb + dx, dy dz)
+  float4* irow;     // ir_mus: ground irradiance row (the two sampler rows pre-blended)
+  float* col_mus;   // S
+  double* col_musd; // S (MIXED)
+  double2* ymu;     // chunk (MIXED): (mu, 1 - mu^2)
+  double* nuraw;    // sc_nu (MIXED)
+  double* acc;      // kDensThreads * kDensMaxGroup * 3 (MIXED: FP64 sum over theta rows)
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
-__host__ __device__ inline size_t dens_layout(unsigned char* base, int dens_n, int sc_nu, int ir_mus, int chunk,
-                                              bool two, DensLayout* L) {
-  const int NT = dens_n, ND = 2 * dens_n * dens_n, NK = sc_nu + 2;
+__host__ __device__ inline size_t dens_layout(unsigned char* base, int dens_n, int sc_nu, int ir_mus, int S,
+                                              int chunk, bool two, bool mixed, DensLayout* L) {
+  const int NT = dens_n, NK = sc_nu + 2;
   size_t o = 0;
   auto take = [&](size_t bytes) {
     size_t at = o;
     o = align16(o + bytes);
     return at;
   };
-  size_t o_th = take(sizeof(DensTheta) * NT), o_tay = take(sizeof(Axis) * NT), o_kax = take(sizeof(Axis) * NK);
-  size_t o_dir = take(sizeof(float2) * ND), o_gn = take(sizeof(float4) * ND);
-  size_t o_P = take(sizeof(float4) * (size_t)NT * NK * (two ? 2 : 1)), o_irow = take(sizeof(float4) * 2 * ir_mus);
-  size_t o_ymu = take(sizeof(double2) * chunk), o_nu = take(sizeof(double) * sc_nu);
+  size_t o_th = take(sizeof(DensTheta) * NT), o_tay = take(sizeof(Axis) * NT), o_kax = take(sizeof(Axis) * S * NK);
+  size_t o_dir = take(sizeof(float4) * NT * NT), o_gnz = take(sizeof(float) * NT * NT);
+  size_t o_P = take(sizeof(float4) * 2 * (size_t)S * NT * NK * (two ? 2 : 1));
+  size_t o_irow = take(sizeof(float4) * ir_mus);
+  size_t o_cm = take(sizeof(float) * S), o_cmd = take(sizeof(double) * S);
+  size_t o_ymu = take(mixed ? sizeof(double2) * chunk : 0), o_nu = take(mixed ? sizeof(double) * sc_nu : 0);
+  size_t o_acc = take(mixed ? sizeof(double) * kDensThreads * kDensMaxGroup * 3 : 0);
   if (L) {
     L->th = (DensTheta*)(base + o_th);
     L->tay = (Axis*)(base + o_tay);
     L->kax = (Axis*)(base + o_kax);
-    L->dir = (float2*)(base + o_dir);
-    L->gn = (float4*)(base + o_gn);
+    L->dir = (float4*)(base + o_dir);
+    L->gnz = (float*)(base + o_gnz);
     L->P = (float4*)(base + o_P);
     L->irow = (float4*)(base + o_irow);
+    L->col_mus = (float*)(base + o_cm);
+    L->col_musd = (double*)(base + o_cmd);
     L->ymu = (double2*)(base + o_ymu);
     L->nuraw = (double*)(base + o_nu);
+    L->acc = (double*)(base + o_acc);
   }
   return o;
 }
 
+// Phase functions at the scattering angle nu, folded with the per-channel
+// scattering coefficients: (kR kray + kM kmie (1 + g^2 - 2 g nu)^-3/2)(1 + nu^2),
+// i.e. beta_R rho_R P_R(nu) + beta_M rho_M P_M(nu) (util.h:26-34).
+struct PhaseCoef {
+  float3 A, B;  // kR * 3/(16 pi), kM * k_mie
+  float g1, g2;
+  __device__ __forceinline__ float3 eval(float nu, float scale) const {
+    const float t1 = fmaf(nu, nu, 1.0f) * scale;
+    const float rs = rsqrtf(fmaf(-g2, nu, g1));
+    const float rs3 = rs * rs * rs;
+    return make_float3(fmaf(B.x, rs3, A.x) * t1, fmaf(B.y, rs3, A.y) * t1, fmaf(B.z, rs3, A.z) * t1);
+  }
+};
+
 template <bool MX>
-__device__ void tile_density(const DevAtmo& a, int order, int chunk, int tile, unsigned char* smem) {
-  const int NT = a.dens_n, NP = 2 * NT, ND = NT * NP;
-  const int NNU = a.sc_nu, NK = NNU + 2;  // slices -1 .. NNU
-  const int nchunks = (a.sc_mu + chunk - 1) / chunk;
-  const int zi = tile / (a.sc_mus * nchunks);
-  const int rem = tile % (a.sc_mus * nchunks);
-  const int si = rem / nchunks, ci = rem % nchunks;
-  const int y_begin = ci * chunk, y_end = min(a.sc_mu, y_begin + chunk);
+__device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned char* smem) {
+  const int NT = a.dens_n, NNU = a.sc_nu, NK = NNU + 2;
+  const DensShape sh = dens_shape(a.sc_r, a.sc_mu, a.sc_mus, a.sc_nu, a.dens_S, a.dens_chunk);
+  const int zi = tile / (sh.scols * sh.ychunks);
+  const int rem = tile % (sh.scols * sh.ychunks);
+  const int s0 = (rem / sh.ychunks) * sh.S, y0 = (rem % sh.ychunks) * sh.chunk;
+  const int ns = min(sh.S, a.sc_mus - s0), ny = min(sh.chunk, a.sc_mu - y0);
   const bool two = (order - 1) == 1;  // order 2 reads the single Rayleigh/Mie tables
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, nth = blockDim.x;
   DensLayout S;
-  dens_layout(smem, NT, NNU, a.ir_mus, chunk, two, &S);
+  dens_layout(smem, NT, NNU, a.ir_mus, sh.S, sh.chunk, two, MX, &S);
 
   __shared__ Axis s_az, s_irx;
-  __shared__ float s_r, s_mu_s, s_ums;
-  __shared__ double s_q, s_ymus, s_musd, s_omus2;
+  __shared__ float s_r;
+  __shared__ double s_q;
+  // --- tile scalars: r and its axis (z); the ground irradiance row axis
   if (tid == 0) {
-    float r, mu_s, u_ms;
     if (!MX) {
       Geo32 G;
       G.init(a);
-      float mu, nu;
+      float r, mu, mu_s, nu;
       bool g;
-      decode_texel32(a, G, (uint32_t)si, 0u, (uint32_t)zi, r, mu, mu_s, nu, g);
+      decode_texel32(a, G, (uint32_t)s0, 0u, (uint32_t)zi, r, mu, mu_s, nu, g);
+      s_r = r;
       s_az = make_axis(G.u_r(a, r), a.sc_r);
-      u_ms = G.u_mu_s(a, mu_s);
-      s_omus2 = 0.0;
-      s_musd = mu_s;
+      // irradiance at the ground: irradiance.h:20-30 with r = bottom (x_r = 0)
+      s_irx = make_axis(coord_from_unit((a.bottom - a.bottom) / (a.top - a.bottom), a.ir_r), a.ir_r);
     } else {
       Geo64 G;
       G.init(a);
-      TexelParams tp = decode_texel64(a, G, (uint32_t)si, 0u, (uint32_t)zi);
-      r = (float)tp.r;
-      mu_s = (float)tp.mu_s;
+      TexelParams tp = decode_texel64(a, G, (uint32_t)s0, 0u, (uint32_t)zi);
+      s_r = (float)tp.r;
       s_q = tp.q;
       s_az = axis_texel(G.sc_r_texel(a, tp.q), a.sc_r);
-      s_ymus = G.mus_unit(a, tp.mu_s);
-      u_ms = 0.f;
-      s_omus2 = (1.0 - tp.mu_s) * (1.0 + tp.mu_s);
-      s_musd = tp.mu_s;
+      s_irx = axis_texel(0.0f, a.ir_r);
     }
-    s_r = r;
-    s_mu_s = mu_s;
-    s_ums = u_ms;
-    // irradiance at the ground: irradiance.h:20-30 with r = bottom (x_r = 0)
-    s_irx = MX ? axis_texel(0.0f, a.ir_r)
-               : make_axis(coord_from_unit((a.bottom - a.bottom) / (a.top - a.bottom), a.ir_r), a.ir_r);
   }
   __syncthreads();
   const float r = s_r;
-  const Axis az = s_az;
-  // --- per theta: ground flag, ground distance and transmittance, mu axis
-  if (tid < NT) {
-    const int l = tid;
-    DensTheta& o = S.th[l];
-    if (!MX) {
-      Geo32 G;
-      G.init(a);
-      const float dtheta = kPiF / float(NT), dphi = kPiF / float(NT);
-      const float theta = (float(l) + 0.5f) * dtheta;
-      const float ct = cosf(theta);
-      const bool g = G.hits_ground(r, ct);
-      float3 tg = make_float3(0.f, 0.f, 0.f);
-      float dg = 0.0f;
-      if (g) {
-        dg = G.dist_bottom(r, ct);
-        tg = G.tr_segment(a, r, ct, dg, true) * ld3(a.albedo) * (1.0f / kPiF);
+  // --- per theta, per column, per mu row / nu (MIXED decode tables)
+  for (int k = tid; k < NT + ns + (MX ? ny + NNU : 0); k += nth) {
+    if (k < NT) {
+      const int l = k;
+      DensTheta& o = S.th[l];
+      if (!MX) {
+        Geo32 G;
+        G.init(a);
+        const float dtheta = kPiF / float(NT), dphi = kPiF / float(NT);
+        const float theta = (float(l) + 0.5f) * dtheta;
+        const float ct = cosf(theta);
+        const bool g = G.hits_ground(r, ct);
+        float3 tg = make_float3(0.f, 0.f, 0.f);
+        float dg = 0.0f;
+        if (g) {
+          dg = G.dist_bottom(r, ct);
+          tg = G.tr_segment(a, r, ct, dg, true) * ld3(a.albedo) * (1.0f / kPiF);
+        }
+        o.cos_t = ct;
+        o.domega = dtheta * dphi * sinf(theta);
+        o.dg = dg;
+        o.ground = g;
+        o.tgx = tg.x;
+        o.tgy = tg.y;
+        o.tgz = tg.z;
+        S.tay[l] = make_axis(G.u_mu(a, r, ct, g), a.sc_mu);
+      } else {
+        Geo64 G;
+        G.init(a);
+        const double dtheta = kPiD / double(NT), dphi = kPiD / double(NT);
+        const double theta = (double(l) + 0.5) * dtheta;
+        const double ct = cos(theta);
+        const double q = s_q, sv = G.radius(q) * ct;
+        const bool g = G.hits_ground(q, sv);
+        float3 tg = make_float3(0.f, 0.f, 0.f);
+        double dg = 0.0;
+        if (g) {
+          dg = G.dist_bottom(q, sv);
+          tg = G.tr_segment(a, q, sv, dg, true) * ld3(a.albedo) * (float)(1.0 / kPiD);
+        }
+        o.cos_t = (float)ct;
+        o.domega = (float)(dtheta * dphi * sin(theta));
+        o.dg = (float)dg;
+        o.ground = g;
+        o.tgx = tg.x;
+        o.tgy = tg.y;
+        o.tgz = tg.z;
+        S.tay[l] = axis_texel(G.sc_mu_texel(a, q, sv, g), a.sc_mu);
       }
-      o.cos_t = ct;
-      o.domega = dtheta * dphi * sinf(theta);
-      o.dg = dg;
-      o.ground = g;
-      o.tgx = tg.x;
-      o.tgy = tg.y;
-      o.tgz = tg.z;
-      S.tay[l] = make_axis(G.u_mu(a, r, ct, g), a.sc_mu);
-    } else {
+    } else if (k < NT + ns) {
+      const int c = k - NT, si = s0 + c;
+      if (!MX) {
+        Geo32 G;
+        G.init(a);
+        float rr, mu, mu_s, nu;
+        bool g;
+        decode_texel32(a, G, (uint32_t)si, 0u, (uint32_t)zi, rr, mu, mu_s, nu, g);
+        S.col_mus[c] = mu_s;
+        const float u_ms = G.u_mu_s(a, mu_s);
+        for (int j = 0; j < NK; ++j) S.kax[c * NK + j] = make_axis((float(j - 1) + u_ms) / float(NNU), a.W);
+      } else {
+        Geo64 G;
+        G.init(a);
+        double mu_s, nu;
+        decode_mus_nu64(a, G, si, mu_s, nu);
+        S.col_mus[c] = (float)mu_s;
+        S.col_musd[c] = mu_s;
+        const double y = G.mus_unit(a, mu_s);
+        for (int j = 0; j < NK; ++j)
+          S.kax[c * NK + j] = axis_texel(double(j - 1) * a.sc_mus + y * double(a.sc_mus - 1), a.W);
+      }
+    } else if (MX) {
       Geo64 G;
       G.init(a);
-      const double dtheta = kPiD / double(NT), dphi = kPiD / double(NT);
-      const double theta = (double(l) + 0.5) * dtheta;
-      const double ct = cos(theta);
-      const double q = s_q, s = G.radius(q) * ct;
-      const bool g = G.hits_ground(q, s);
-      float3 tg = make_float3(0.f, 0.f, 0.f);
-      double dg = 0.0;
-      if (g) {
-        dg = G.dist_bottom(q, s);
-        tg = G.tr_segment(a, q, s, dg, true) * ld3(a.albedo) * (float)(1.0 / kPiD);
-      }
-      o.cos_t = (float)ct;
-      o.domega = (float)(dtheta * dphi * sin(theta));
-      o.dg = (float)dg;
-      o.ground = g;
-      o.tgx = tg.x;
-      o.tgy = tg.y;
-      o.tgz = tg.z;
-      S.tay[l] = axis_texel(G.sc_mu_texel(a, q, s, g), a.sc_mu);
-    }
-  }
-  if (tid >= 64 && tid < 64 + NK) {
-    const int k = tid - 64;
-    S.kax[k] = MX ? axis_texel(double(k - 1) * a.sc_mus + s_ymus * double(a.sc_mus - 1), a.W)
-                  : make_axis((float(k - 1) + s_ums) / float(NNU), a.W);
-  }
-  if (MX && tid >= 128) {
-    Geo64 G;
-    G.init(a);
-    const int nk = (y_end - y_begin) + NNU;
-    for (int k = tid - 128; k < nk; k += kThreads - 128) {
-      if (k < y_end - y_begin) {
-        TexelParams tp = decode_texel64(a, G, (uint32_t)si, (uint32_t)(y_begin + k), (uint32_t)zi);
-        S.ymu[k] = make_double2(tp.mu, (1.0 - tp.mu) * (1.0 + tp.mu));
+      const int k2 = k - NT - ns;
+      if (k2 < ny) {
+        TexelParams tp = decode_texel64(a, G, (uint32_t)s0, (uint32_t)(y0 + k2), (uint32_t)zi);
+        S.ymu[k2] = make_double2(tp.mu, (1.0 - tp.mu) * (1.0 + tp.mu));
       } else {
-        const int n = k - (y_end - y_begin);
+        const int n = k2 - ny;
         double mu_s, nu;
-        decode_mus_nu64(a, G, n * a.sc_mus + si, mu_s, nu);
+        decode_mus_nu64(a, G, n * a.sc_mus, mu_s, nu);
         S.nuraw[n] = nu;
       }
     }
   }
   __syncthreads();
-  // --- reduced table P[theta][slice], directions, ground normals, ground irradiance
+  // --- reduced tables, direction pairs with ground normals, ground irradiance row
   {
     const float4* src0 = two ? a.dr : a.dms;
-    for (int k = tid; k < NT * NK; k += kThreads) {
-      const int l = k / NK, s = k % NK;
-      const float3 v = fetch3(src0, a.W, a.sc_mu, S.kax[s], S.tay[l], az);
-      S.P[k] = make_float4(v.x, v.y, v.z, 0.f);
+    const int per_col = NT * NK;
+    for (int k = tid; k < ns * per_col; k += nth) {
+      const int c = k / per_col, l = (k % per_col) / NK, sl = k % NK;
+      const int slc = min(sl + 1, NK - 1);
+      const float3 v0 = fetch3(src0, a.W, a.sc_mu, S.kax[c * NK + sl], S.tay[l], s_az);
+      const float3 v1 = sl + 1 < NK ? fetch3(src0, a.W, a.sc_mu, S.kax[c * NK + slc], S.tay[l], s_az) : v0;
+      S.P[2 * k] = make_float4(v0.x, v0.y, v0.z, v1.x - v0.x);
+      S.P[2 * k + 1] = make_float4(v1.y - v0.y, v1.z - v0.z, 0.f, 0.f);
       if (two) {
-        const float3 m = fetch3(a.dm, a.W, a.sc_mu, S.kax[s], S.tay[l], az);
-        S.P[NT * NK + k] = make_float4(m.x, m.y, m.z, 0.f);
+        const float3 m0 = fetch3(a.dm, a.W, a.sc_mu, S.kax[c * NK + sl], S.tay[l], s_az);
+        const float3 m1 = sl + 1 < NK ? fetch3(a.dm, a.W, a.sc_mu, S.kax[c * NK + slc], S.tay[l], s_az) : m0;
+        const size_t off = 2 * (size_t)sh.S * per_col;
+        S.P[off + 2 * k] = make_float4(m0.x, m0.y, m0.z, m1.x - m0.x);
+        S.P[off + 2 * k + 1] = make_float4(m1.y - m0.y, m1.z - m0.z, 0.f, 0.f);
       }
     }
     const float dtheta = kPiF / float(NT), dphi = kPiF / float(NT);
-    for (int k = tid; k < ND; k += kThreads) {
-      const int l = k / NP, m = k % NP;
-      const float theta = (float(l) + 0.5f) * dtheta;
-      const float st = sinf(theta);
+    for (int k = tid; k < NT * NT; k += nth) {
+      const int l = k / NT, m = k % NT;
+      const float st = sinf((float(l) + 0.5f) * dtheta);
       const float phi = (float(m) + 0.5f) * dphi;
       const float cx = cosf(phi) * st, cy = sinf(phi) * st;
-      S.dir[k] = make_float2(cx, cy);
       // normalize(zenith * r + omega_i * distance_to_ground)
       const float dg = S.th[l].dg, ct = S.th[l].cos_t;
       const float gx = cx * dg, gy = cy * dg, gz = r + ct * dg;
       const float len = sqrtf(gx * gx + gy * gy + gz * gz);
-      S.gn[k] = make_float4(gx / len, gy / len, gz / len, 0.f);
+      S.dir[k] = make_float4(cx, cy, gx / len, gy / len);
+      S.gnz[k] = gz / len;
     }
     const float4* E = a.dirr[order & 1];  // irradiance of order n-2
-    for (int k = tid; k < 2 * a.ir_mus; k += kThreads) {
-      const int row = k < a.ir_mus ? s_irx.i0 : s_irx.i1;
-      S.irow[k] = E[row * a.ir_mus + (k % a.ir_mus)];
+    const float fy = s_irx.f;
+    for (int k = tid; k < a.ir_mus; k += nth) {
+      const float4 e0 = E[s_irx.i0 * a.ir_mus + k], e1 = E[s_irx.i1 * a.ir_mus + k];
+      S.irow[k] = make_float4(fmaf(e1.x - e0.x, fy, e0.x), fmaf(e1.y - e0.y, fy, e0.y), fmaf(e1.z - e0.z, fy, e0.z),
+                              0.f);
     }
   }
   __syncthreads();
 
-  // --- texels of the tile: (nu, mu) pairs at the tile's (r, mu_s)
-  const float h0 = r - a.bottom;
-  const float rho_r = profile_density(a.ray_d, h0), rho_m = profile_density(a.mie_d, h0);
-  const float3 kR = make_float3(a.rayleigh[0] * rho_r, a.rayleigh[1] * rho_r, a.rayleigh[2] * rho_r);
-  const float3 kM = make_float3(a.mie_sca[0] * rho_m, a.mie_sca[1] * rho_m, a.mie_sca[2] * rho_m);
-  const float g = a.g;
-  const float kmie = 3.0f / (8.0f * kPiF) * (1.0f - g * g) / (2.0f + g * g);
-  const float kray = 3.0f / (16.0f * kPiF);
-  const float g1 = 1.0f + g * g, g2 = 2.0f * g;
-  const float fnu = float(NNU - 1);
-  const Axis irx = s_irx;
-  const int ntex = (y_end - y_begin) * NNU;
-  for (int k = tid; k < ntex; k += kThreads) {
-    const int nu_i = k % NNU, y = y_begin + k / NNU;
-    const int x = nu_i * a.sc_mus + si;
-    float mu, mu_s, ox, sx, sy;
-    if (!MX) {
-      Geo32 G;
-      G.init(a);
-      float rr, nu;
-      bool gg;
-      decode_texel32(a, G, (uint32_t)x, (uint32_t)y, (uint32_t)zi, rr, mu, mu_s, nu, gg);
-      // scattering_density.comp:28-32
-      ox = sqrtf(1.0f - mu * mu);
-      sx = ox == 0.0f ? 0.0f : (nu - mu * mu_s) / ox;
-      sy = sqrtf(gmax(1.0f - sx * sx - mu_s * mu_s, 0.0f));
-    } else {
-      // The same frame in FP64, with nu clamped (scattering.h:134-136) as
-      // delta = nu - mu mu_s in [-sq, sq], sq = sqrt((1-mu^2)(1-mu_s^2)), and
-      // sun_y^2 = (sq - delta)(sq + delta) / (1 - mu^2): exactly 0 when the sun
-      // lies in the view plane, where 1 - sun_x^2 - mu_s^2 would cancel.
-      const double2 ym = S.ymu[y - y_begin];
-      const double mud = ym.x, om = ym.y, musd = s_musd;
-      const double sq = sqrt(om * s_omus2), mm = mud * musd;
-      const double delta = gclamp(S.nuraw[nu_i] - mm, -sq, sq);
-      double sxd, syd;
-      if (om == 0.0) {
-        sxd = 0.0;
-        syd = sqrt(gmax(s_omus2, 0.0));
-      } else {
-        sxd = delta / sqrt(om);
-        syd = sqrt(gmax((sq - delta) * (sq + delta), 0.0) / om);
+  // --- this thread's nu group
+  const int per_s = sh.chunk * sh.NG;
+  const int cl = tid / per_s, yl = (tid % per_s) / sh.NG, grp = tid % sh.NG;
+  const bool active = tid < sh.S * per_s && cl < ns && yl < ny;
+  if (active) {
+    const int G = sh.G, y = y0 + yl, si = s0 + cl;
+    float mu, ox, mu_s;
+    float sx[kDensMaxGroup], sy[kDensMaxGroup];
+#pragma unroll
+    for (int j = 0; j < kDensMaxGroup; ++j) {
+      sx[j] = sy[j] = 0.f;
+      if (j < G) {
+        const int nu_i = grp * G + j, x = nu_i * a.sc_mus + si;
+        if (!MX) {
+          Geo32 Gm;
+          Gm.init(a);
+          float rr, ms, nu;
+          bool gg;
+          decode_texel32(a, Gm, (uint32_t)x, (uint32_t)y, (uint32_t)zi, rr, mu, ms, nu, gg);
+          // scattering_density.comp:28-32
+          ox = sqrtf(1.0f - mu * mu);
+          sx[j] = ox == 0.0f ? 0.0f : (nu - mu * ms) / ox;
+          sy[j] = sqrtf(gmax(1.0f - sx[j] * sx[j] - ms * ms, 0.0f));
+        } else {
+          // the same frame in FP64, nu clamped (scattering.h:134-136) as
+          // delta = nu - mu mu_s in [-sq, sq]; sun_y^2 = (sq - delta)(sq + delta)
+          // / (1 - mu^2) is exactly 0 when the sun lies in the view plane
+          const double2 ym = S.ymu[yl];
+          const double mud = ym.x, om = ym.y, musd = S.col_musd[cl];
+          const double omus = (1.0 - musd) * (1.0 + musd);
+          const double sq = sqrt(om * omus), mm = mud * musd;
+          const double delta = gclamp(S.nuraw[nu_i] - mm, -sq, sq);
+          if (om == 0.0) {
+            sx[j] = 0.f;
+            sy[j] = (float)sqrt(gmax(omus, 0.0));
+          } else {
+            sx[j] = (float)(delta / sqrt(om));
+            sy[j] = (float)sqrt(gmax((sq - delta) * (sq + delta), 0.0) / om);
+          }
+          mu = (float)mud;
+          ox = (float)sqrt(om);
+        }
       }
-      mu = (float)mud;
-      mu_s = (float)musd;
-      ox = (float)sqrt(om);
-      sx = (float)sxd;
-      sy = (float)syd;
     }
-    Kahan3 acc;
-    acc.init();
+    mu_s = S.col_mus[cl];
+    const float h0 = r - a.bottom;
+    const float rho_r = profile_density(a.ray_d, h0), rho_m = profile_density(a.mie_d, h0);
+    const float g = a.g;
+    const float kmie = 3.0f / (8.0f * kPiF) * (1.0f - g * g) / (2.0f + g * g);
+    const float kray = 3.0f / (16.0f * kPiF);
+    PhaseCoef pc;
+    pc.A = make_float3(a.rayleigh[0] * rho_r * kray, a.rayleigh[1] * rho_r * kray, a.rayleigh[2] * rho_r * kray);
+    pc.B = make_float3(a.mie_sca[0] * rho_m * kmie, a.mie_sca[1] * rho_m * kmie, a.mie_sca[2] * rho_m * kmie);
+    pc.g1 = 1.0f + g * g;
+    pc.g2 = 2.0f * g;
+    const float hf = 0.5f * float(NNU - 1);
+    const float fmaxk = float(NNU - 1);
+    // ground irradiance row coordinate: u = coord(mg / 2 + 1/2), texel u n - 1/2
+    const float ir_c0 = 0.5f / float(a.ir_mus), ir_c1 = 1.0f - 1.0f / float(a.ir_mus), ir_n = float(a.ir_mus);
+    float3 acc[kDensMaxGroup];
+#pragma unroll
+    for (int j = 0; j < kDensMaxGroup; ++j) acc[j] = make_float3(0.f, 0.f, 0.f);
+    double* accd = S.acc + (size_t)tid * kDensMaxGroup * 3;
+    if (MX) {
+      for (int j = 0; j < 3 * kDensMaxGroup; ++j) accd[j] = 0.0;
+    }
+    const size_t ptab = 2 * (size_t)sh.S * NT * NK;
     for (int l = 0; l < NT; ++l) {
       const DensTheta t = S.th[l];
-      const float4* Pl = S.P + l * NK;
-      const float4* Ml = S.P + NT * NK + l * NK;
       const float mus_ct = mu_s * t.cos_t, mu_ct = mu * t.cos_t;
-      Kahan3 accl;
-      accl.init();
-      for (int m = 0; m < NP; ++m) {
-        const float2 c = S.dir[l * NP + m];
-        // incident radiance of order n-1 (scattering.h:139-179)
-        const float nu1 = sx * c.x + sy * c.y + mus_ct;
-        const float tcx = (nu1 + 1.0f) / 2.0f * fnu;
-        float fk = floorf(tcx);
-        const float lf = tcx - fk;
-        fk = fminf(fmaxf(fk, -1.0f), float(NNU - 1));
-        const int ks = (int)fk + 1;
-        float3 inc;
-        if (two) {
-          const float4 r0 = Pl[ks], r1 = Pl[ks + 1], m0 = Ml[ks], m1 = Ml[ks + 1];
-          const float pr = kray * (1.0f + nu1 * nu1);
-          const float rs = rsqrtf(g1 - g2 * nu1);
-          const float pm = kmie * (1.0f + nu1 * nu1) * (rs * rs * rs);
-          inc.x = fmaf(r1.x - r0.x, lf, r0.x) * pr + fmaf(m1.x - m0.x, lf, m0.x) * pm;
-          inc.y = fmaf(r1.y - r0.y, lf, r0.y) * pr + fmaf(m1.y - m0.y, lf, m0.y) * pm;
-          inc.z = fmaf(r1.z - r0.z, lf, r0.z) * pr + fmaf(m1.z - m0.z, lf, m0.z) * pm;
-        } else {
-          const float4 r0 = Pl[ks], r1 = Pl[ks + 1];
-          inc.x = fmaf(r1.x - r0.x, lf, r0.x);
-          inc.y = fmaf(r1.y - r0.y, lf, r0.y);
-          inc.z = fmaf(r1.z - r0.z, lf, r0.z);
-        }
-        if (t.ground) {
-          // ground bounce: irradiance of order n-2 at the ground point
-          const float4 nrm = S.gn[l * NP + m];
-          const float mg = nrm.x * sx + nrm.y * sy + nrm.z * mu_s;
-          const Axis ax = MX ? axis_texel((mg * 0.5f + 0.5f) * float(a.ir_mus - 1), a.ir_mus)
-                             : make_axis(coord_from_unit(mg * 0.5f + 0.5f, a.ir_mus), a.ir_mus);
-          const float4 e00 = S.irow[ax.i0], e10 = S.irow[ax.i1];
-          const float4 e01 = S.irow[a.ir_mus + ax.i0], e11 = S.irow[a.ir_mus + ax.i1];
-          const float w00 = (1.f - ax.f) * (1.f - irx.f), w10 = ax.f * (1.f - irx.f);
-          const float w01 = (1.f - ax.f) * irx.f, w11 = ax.f * irx.f;
-          inc.x = fmaf(t.tgx, w00 * e00.x + w10 * e10.x + w01 * e01.x + w11 * e11.x, inc.x);
-          inc.y = fmaf(t.tgy, w00 * e00.y + w10 * e10.y + w01 * e01.y + w11 * e11.y, inc.y);
-          inc.z = fmaf(t.tgz, w00 * e00.z + w10 * e10.z + w01 * e01.z + w11 * e11.z, inc.z);
-        }
-        // phase functions of the scattering angle omega . omega_i
-        const float nu2 = ox * c.x + mu_ct;
-        const float pr2 = kray * (1.0f + nu2 * nu2);
-        const float rs2 = rsqrtf(g1 - g2 * nu2);
-        const float pm2 = kmie * (1.0f + nu2 * nu2) * (rs2 * rs2 * rs2);
-        float3 v;
-        v.x = inc.x * fmaf(kR.x, pr2, kM.x * pm2);
-        v.y = inc.y * fmaf(kR.y, pr2, kM.y * pm2);
-        v.z = inc.z * fmaf(kR.z, pr2, kM.z * pm2);
-        if (!MX) {
-          accl.s.x += v.x;
-          accl.s.y += v.y;
-          accl.s.z += v.z;
-        } else {
-          accl.add(v);
+      const float4* Pl = S.P + 2 * (size_t)((cl * NT + l) * NK);
+      const float4* Ml = Pl + ptab;
+      for (int m = 0; m < NT; ++m) {
+        const float4 d = S.dir[l * NT + m];
+        // phase functions of omega . omega_i, shared by the pair and the group
+        const float nu2 = fmaf(ox, d.x, mu_ct);
+        const float3 cf = pc.eval(nu2, t.domega);
+        const float gzm = t.ground ? S.gnz[l * NT + m] * mu_s : 0.f;
+#pragma unroll
+        for (int j = 0; j < kDensMaxGroup; ++j) {
+          if (j < G) {
+            const float base = fmaf(sx[j], d.x, mus_ct), dy = sy[j] * d.y;
+            const float gb = fmaf(d.z, sx[j], gzm), gdy = d.w * sy[j];
+#pragma unroll
+            for (int side = 0; side < 2; ++side) {
+              // incident radiance of order n-1 (scattering.h:139-179)
+              const float nu1 = side ? base - dy : base + dy;
+              const float tcx = fmaf(nu1, hf, hf);
+              float fk = floorf(tcx);
+              const float lf = tcx - fk;
+              fk = fminf(fmaxf(fk, -1.0f), fmaxk);
+              const int ks = 2 * ((int)fk + 1);
+              const float4 p0 = Pl[ks], p1 = Pl[ks + 1];
+              float3 inc = make_float3(fmaf(p0.w, lf, p0.x), fmaf(p1.x, lf, p0.y), fmaf(p1.y, lf, p0.z));
+              if (two) {
+                const float4 q0 = Ml[ks], q1 = Ml[ks + 1];
+                const float pr = kray * fmaf(nu1, nu1, 1.0f);
+                const float rs = rsqrtf(fmaf(-pc.g2, nu1, pc.g1));
+                const float pm = kmie * fmaf(nu1, nu1, 1.0f) * (rs * rs * rs);
+                inc.x = fmaf(fmaf(q0.w, lf, q0.x), pm, inc.x * pr);
+                inc.y = fmaf(fmaf(q1.x, lf, q0.y), pm, inc.y * pr);
+                inc.z = fmaf(fmaf(q1.y, lf, q0.z), pm, inc.z * pr);
+              }
+              if (t.ground) {
+                // ground bounce: irradiance of order n-2 where omega_i meets the ground
+                const float mg = side ? gb - gdy : gb + gdy;
+                float tx;
+                if (!MX) tx = fmaf(fmaf(fmaf(mg, 0.5f, 0.5f), ir_c1, ir_c0), ir_n, -0.5f);
+                else tx = fmaf(mg, 0.5f, 0.5f) * float(a.ir_mus - 1);
+                const Axis ax = axis_texel(tx, a.ir_mus);
+                const float4 e0 = S.irow[ax.i0], e1 = S.irow[ax.i1];
+                inc.x = fmaf(t.tgx, fmaf(e1.x - e0.x, ax.f, e0.x), inc.x);
+                inc.y = fmaf(t.tgy, fmaf(e1.y - e0.y, ax.f, e0.y), inc.y);
+                inc.z = fmaf(t.tgz, fmaf(e1.z - e0.z, ax.f, e0.z), inc.z);
+              }
+              acc[j].x = fmaf(inc.x, cf.x, acc[j].x);
+              acc[j].y = fmaf(inc.y, cf.y, acc[j].y);
+              acc[j].z = fmaf(inc.z, cf.z, acc[j].z);
+            }
+          }
         }
       }
-      const float3 part = make_float3(accl.s.x - accl.c.x, accl.s.y - accl.c.y, accl.s.z - accl.c.z);
-      if (!MX) acc.s = acc.s + part * t.domega;
-      else acc.add(part * t.domega);
+      if (MX) {
+        // FP64 sum over theta rows of the FP32 sums over one row
+#pragma unroll
+        for (int j = 0; j < kDensMaxGroup; ++j) {
+          if (j < G) {
+            accd[3 * j] += acc[j].x;
+            accd[3 * j + 1] += acc[j].y;
+            accd[3 * j + 2] += acc[j].z;
+            acc[j] = make_float3(0.f, 0.f, 0.f);
+          }
+        }
+      }
     }
-    const float3 o = make_float3(acc.s.x - acc.c.x, acc.s.y - acc.c.y, acc.s.z - acc.c.z);
-    const size_t t = ((size_t)zi * a.sc_mu + y) * a.W + x;
-    a.dens[t] = store_round4(make_float4(o.x, o.y, o.z, 0.f), a.f16);
+#pragma unroll
+    for (int j = 0; j < kDensMaxGroup; ++j) {
+      if (j < G) {
+        const int x = (grp * G + j) * a.sc_mus + si;
+        const size_t tt = ((size_t)zi * a.sc_mu + y) * a.W + x;
+        float3 o = acc[j];
+        if (MX) o = make_float3((float)accd[3 * j], (float)accd[3 * j + 1], (float)accd[3 * j + 2]);
+        a.dens[tt] = store_round4(make_float4(o.x, o.y, o.z, 0.f), a.f16);
+      }
+    }
   }
 }
 
@@ -798,7 +906,7 @@ __device__ void tile_density(const DevAtmo& a, int order, int chunk, int tile, u
 // split the 16 x 64 directions, and warp shuffles plus one shared-memory step
 // sum them.
 __host__ __device__ inline size_t indirect_smem(int irr_n, int sc_nu, bool one) {
-  return sizeof(float4) * (size_t)(irr_n / 2) * (sc_nu + 2) * (one ? 2 : 1) + sizeof(double) * 3 * (kThreads / 32);
+  return sizeof(float4) * (size_t)(irr_n / 2) * (sc_nu + 2) * (one ? 2 : 1) + sizeof(double) * 3 * 32;
 }
 
 template <bool MX>
@@ -837,7 +945,8 @@ __device__ void tile_indirect(const DevAtmo& a, int order, int tile, unsigned ch
   }
   const float4* src0 = one ? a.dr : a.dms;
   const float dthetaf = kPiF / float(a.irr_n), dphif = kPiF / float(a.irr_n);
-  for (int k = tid; k < NT * NK; k += kThreads) {
+  const int nth = blockDim.x;
+  for (int k = tid; k < NT * NK; k += nth) {
     const int l = k / NK, s = k % NK;
     Axis ay, ax;
     if (!MX) {
@@ -869,7 +978,7 @@ __device__ void tile_indirect(const DevAtmo& a, int order, int tile, unsigned ch
   const float fnu = float(NNU - 1);
   Kahan3 acc;
   acc.init();
-  for (int k = tid; k < NT * NP; k += kThreads) {
+  for (int k = tid; k < NT * NP; k += nth) {
     const int l = k / NP, m = k % NP;
     const float theta = (float(l) + 0.5f) * dthetaf, phi = (float(m) + 0.5f) * dphif;
     const float st = sinf(theta);
@@ -920,7 +1029,7 @@ __device__ void tile_indirect(const DevAtmo& a, int order, int tile, unsigned ch
   __syncthreads();
   if (tid == 0) {
     double tx = 0, ty = 0, tz = 0;
-    for (int w = 0; w < kThreads / 32; ++w) {
+    for (int w = 0; w < nth / 32; ++w) {
       tx += red[3 * w];
       ty += red[3 * w + 1];
       tz += red[3 * w + 2];
@@ -940,11 +1049,11 @@ __device__ void tile_indirect(const DevAtmo& a, int order, int tile, unsigned ch
   }
 }
 
-template <bool MX> __global__ void __launch_bounds__(kThreads) k_density(LaunchArgs L) {
+template <bool MX> __global__ void __launch_bounds__(kDensThreads, 4) k_density(LaunchArgs L) {
   extern __shared__ __align__(16) unsigned char smem[];
   int seg, job, tile;
   while (next_item(L, seg, job, tile)) {
-    if (seg == 0) tile_density<MX>(L.atm[job], L.order, L.atm[job].dens_chunk, tile, smem);
+    if (seg == 0) tile_density<MX>(L.atm[job], L.order, tile, smem);
     else tile_indirect<MX>(L.atm[job], L.order, tile, smem);
   }
 }
@@ -957,7 +1066,7 @@ template <bool MX> __global__ void __launch_bounds__(kThreads) k_density(LaunchA
 // once into a slab over x; each texel then blends four slab entries (two
 // mu_s neighbours in two nu slices).
 struct MSRec {
-  float d, r_i, wdx, tvx, tvy, tvz, fy, fz;
+  float d, inv_r, wdx, tvx, tvy, tvz, fy, fz;
   int y0, y1, z0, z1;
 };
 
@@ -1004,7 +1113,7 @@ __device__ void tile_multiple(const DevAtmo& a, int tile, unsigned char* smem) {
       az = make_axis(G.u_r(a, r_i), a.sc_r);
       ay = make_axis(G.u_mu(a, r_i, mu_i, ri.ground), a.sc_mu);
       o.d = d;
-      o.r_i = r_i;
+      o.inv_r = 1.0f / r_i;
     } else {
       Geo64 G;
       G.init(a);
@@ -1015,7 +1124,7 @@ __device__ void tile_multiple(const DevAtmo& a, int tile, unsigned char* smem) {
       az = axis_texel(G.sc_r_texel(a, q), a.sc_r);
       ay = axis_texel(G.sc_mu_texel(a, q, s, ri.ground), a.sc_mu);
       o.d = (float)d;
-      o.r_i = (float)G.radius(q);
+      o.inv_r = (float)(1.0 / G.radius(q));
     }
     o.wdx = ri.dx * w;
     o.tvx = tv.x;
@@ -1034,8 +1143,8 @@ __device__ void tile_multiple(const DevAtmo& a, int tile, unsigned char* smem) {
   Kahan3 acc[TPT];
   MuS32 mus32;
   mus32.init(a);
-  Geo32 G32;
-  G32.init(a);
+  MuSRef32 musref;
+  musref.init(a);
 #pragma unroll
   for (int j = 0; j < TPT; ++j) {
     acc[j].init();
@@ -1076,7 +1185,7 @@ __device__ void tile_multiple(const DevAtmo& a, int tile, unsigned char* smem) {
   };
   build(0, slab);
   __syncthreads();
-  const float fnu = float(a.sc_nu);
+  const float fmus = float(a.sc_mus);
   for (int i = 0; i < NS; ++i) {
     const float4* cur = slab + (i & 1) * slab_stride;
     if (i + 1 < NS) build(i + 1, slab + ((i + 1) & 1) * slab_stride);
@@ -1091,16 +1200,17 @@ __device__ void tile_multiple(const DevAtmo& a, int tile, unsigned char* smem) {
         const float tx = c_tex[j];
         Axis x0, x1;
         if (!MX) {
-          const float mu_s_i = clamp_cosine((c_rmus[j] + o.d * nu) / o.r_i);
-          const float u_ms = G32.u_mu_s(a, mu_s_i);
-          x0 = make_axis((tx + u_ms) / fnu, W);
-          x1 = make_axis((tx + 1.0f + u_ms) / fnu, W);
+          // sampler coordinate ((tex_x + u_mu_s) / nu_size) W - 1/2 (scattering.h:149-151)
+          const float mu_s_i = clamp_cosine((c_rmus[j] + o.d * nu) * o.inv_r);
+          const float t = fmaf(tx + musref.coord(mu_s_i), fmus, -0.5f);
+          x0 = axis_texel(t, W);
+          x1 = axis_texel(t + fmus, W);
         } else {
           // texel coordinate of slice k: k * mu_s_size + y (mu_s_size - 1)
-          const float mu_s_i = clamp_cosine(fmaf(o.d, nu, c_rmus[j]) / o.r_i);
+          const float mu_s_i = clamp_cosine(fmaf(o.d, nu, c_rmus[j]) * o.inv_r);
           const float t = mus32.texel(mu_s_i);
-          x0 = axis_texel(fmaf(tx, float(a.sc_mus), t), W);
-          x1 = axis_texel(fmaf(tx + 1.0f, float(a.sc_mus), t), W);
+          x0 = axis_texel(fmaf(tx, fmus, t), W);
+          x1 = axis_texel(fmaf(tx + 1.0f, fmus, t), W);
         }
         const float4* sl = cur + lr * W;
         const float4 p00 = sl[x0.i0], p01 = sl[x0.i1], p10 = sl[x1.i0], p11 = sl[x1.i1];
@@ -1158,16 +1268,17 @@ __host__ __device__ inline int tiles_rows(int W, int sc_mu, int sc_r) {
 }
 __host__ __device__ inline int tiles_direct(int ir_mus, int ir_r) { return (ir_mus * ir_r + kThreads - 1) / kThreads; }
 __host__ __device__ inline int tiles_indirect(int ir_mus, int ir_r) { return ir_mus * ir_r; }
-__host__ __device__ inline int tiles_density(int sc_r, int sc_mus, int sc_mu, int chunk) {
-  return sc_r * sc_mus * ((sc_mu + chunk - 1) / chunk);
+__host__ __device__ inline int tiles_density(const DevAtmo& a) {
+  return dens_shape(a.sc_r, a.sc_mu, a.sc_mus, a.sc_nu, a.dens_S, a.dens_chunk).tiles;
 }
 __host__ __device__ inline size_t ss_smem(int W, int steps, int sc_mus, int sc_nu) {
   const int R = rows_per_tile(W);
   return sizeof(RowInfo) * R + sizeof(SSRec) * (size_t)R * (steps + 1) + 16 + sizeof(double2) * sc_mus +
          sizeof(double) * sc_nu + 16;
 }
-__host__ __device__ inline size_t density_smem(int dens_n, int sc_nu, int ir_mus, int chunk, bool two) {
-  return dens_layout(nullptr, dens_n, sc_nu, ir_mus, chunk, two, nullptr);
+__host__ __device__ inline size_t density_smem(const DevAtmo& a, bool two, bool mixed) {
+  const DensShape d = dens_shape(a.sc_r, a.sc_mu, a.sc_mus, a.sc_nu, a.dens_S, a.dens_chunk);
+  return dens_layout(nullptr, a.dens_n, a.sc_nu, a.ir_mus, d.S, d.chunk, two, mixed, nullptr);
 }
 
 }  // namespace fb

@@ -31,17 +31,17 @@ cudaError_t launch_to_half(const float4* src, void* dst, size_t n, cudaStream_t 
   return cudaGetLastError();
 }
 
-int default_density_chunk(int sc_mu, int sc_nu) {
-  return std::max(1, std::min(sc_mu, 512 / std::max(1, sc_nu)));
-}
-
 void tuning_load_default(Tuning& t) { t.entries.clear(); }
 
-int tuning_density_chunk(const Tuning& t, int sc_r, int sc_mu, int sc_mus, int sc_nu) {
+void tuning_density_shape(const Tuning& t, int sc_r, int sc_mu, int sc_mus, int sc_nu, int* S, int* chunk) {
+  *S = 0;
+  *chunk = 0;
   for (const TuneEntry& e : t.entries)
-    if (e.sc_r == sc_r && e.sc_mu == sc_mu && e.sc_mus == sc_mus && e.sc_nu == sc_nu)
-      return std::max(1, std::min(sc_mu, e.density_chunk));
-  return default_density_chunk(sc_mu, sc_nu);
+    if (e.sc_r == sc_r && e.sc_mu == sc_mu && e.sc_mus == sc_mus && e.sc_nu == sc_nu) {
+      *S = e.dens_S;
+      *chunk = e.dens_chunk;
+      return;
+    }
 }
 
 }  // namespace fbi

@@ -259,6 +259,63 @@ void fb_atmosphere_destroy(fb_atmosphere* a);
 int fb_batch_build(fb_builder* b, void* stream, const fb_params* params,
                    uint32_t count, fb_pending** out);
 
+/* ---- serving ------------------------------------------------------------- */
+
+/* A request loop over one builder: precompute requests arrive at any time and
+ * are admitted while the device-memory budget allows (in-flight builds plus
+ * resident tables), several batches run at once on separate streams (requests
+ * that arrive while others are on the GPU start without waiting for them),
+ * and finished tables stay resident on the device for renderers, evicted in
+ * least-recently-used order when the budget needs the room. A request for
+ * parameters that are already resident (or in flight) shares that result. */
+typedef struct fb_server fb_server;
+
+typedef struct fb_server_config {
+    uint64_t hbm_budget_bytes; /* device bytes for in-flight builds + resident tables (default 120 GB) */
+    uint32_t max_batch;        /* atmospheres per batch launch (default 64) */
+    uint32_t max_inflight;     /* batches running at once, one stream each (default 4) */
+    uint32_t cache_entries;    /* finished atmospheres kept resident at most (default 4096) */
+    uint32_t max_queue;        /* queued requests beyond which submit refuses (default 65536) */
+    uint32_t reserved[6];
+} fb_server_config;
+
+typedef struct fb_server_stats {
+    uint64_t submitted;      /* requests accepted */
+    uint64_t completed;      /* requests whose tables are ready (built or shared) */
+    uint64_t rejected;       /* refused: over budget alone or queue full */
+    uint64_t cancelled;
+    uint64_t cache_hits;     /* requests answered by resident or in-flight tables */
+    uint64_t evictions;      /* resident atmospheres freed to make room */
+    uint64_t batches;        /* batch launches */
+    uint64_t resident_bytes; /* finished tables on the device */
+    uint64_t inflight_bytes; /* outputs + temporaries of running batches */
+    uint64_t queued;         /* requests waiting for admission */
+    double p50_ms;           /* submit-to-ready latency of completed requests */
+    double p99_ms;
+    double mean_ms;
+    double mean_batch;       /* atmospheres per batch launch */
+} fb_server_stats;
+
+void fb_server_config_default(fb_server_config* out);
+int fb_server_create(fb_builder* b, const fb_server_config* cfg, fb_server** out);
+/* Queues a request; FB_ERR_BUDGET if its tables alone exceed the budget,
+ * FB_ERR_SHUTDOWN after destroy began. */
+int fb_server_submit(fb_server* s, const fb_params* p, uint64_t* ticket);
+/* FB_OK (and *out) when the request's tables are ready, FB_NOT_READY while it
+ * is queued or running, FB_ERR_CANCELLED / FB_ERR_NOT_FOUND otherwise. The
+ * atmosphere stays owned by the server and is not evicted until
+ * fb_server_release(ticket). */
+int fb_server_poll(fb_server* s, uint64_t ticket, fb_atmosphere** out);
+/* As fb_server_poll, blocking up to timeout_ms (UINT32_MAX: no limit). */
+int fb_server_wait(fb_server* s, uint64_t ticket, uint32_t timeout_ms, fb_atmosphere** out);
+/* The caller is done with the ticket's tables; they may now be evicted. */
+int fb_server_release(fb_server* s, uint64_t ticket);
+/* Cancels a request that has not started; FB_NOT_READY if it is running. */
+int fb_server_cancel(fb_server* s, uint64_t ticket);
+int fb_server_get_stats(fb_server* s, fb_server_stats* out);
+/* Waits for running batches, frees every resident table, stops the loop. */
+void fb_server_destroy(fb_server* s);
+
 /* ---- profiling ----------------------------------------------------------- */
 
 /* When enabled, builds record a CUDA timing event around every kernel launch

@@ -172,3 +172,94 @@ int fbref_precompute(const fb_params* p, float* tr, float* ir, float* sc, float*
 }
 
 }  // extern "C"
+
+extern "C" {
+
+// Runs one pass of the reference's shaders for the listed invocations (linear
+// ids x + width * (y + height * z) of the pass's output grid), reading and
+// writing caller-owned full-size RGBA tables. Used to time a bounded sample of
+// the reference's own code. pass: 0 transmittance, 1 direct irradiance,
+// 2 single scattering, 3 scattering density, 4 indirect irradiance,
+// 5 multiple scattering. `order` is the push constant of passes 3 and 4.
+int fbref_run_pass(int pass, const fb_params* p, int order, float* tr, float* dirr, float* dr, float* dm,
+                   float* dms, float* dens, float* ir, float* sc, const int64_t* ids, int64_t n) {
+  if (!p || !ids) return FB_ERR_INVALID_ARGUMENT;
+  const fb_params_raw& r = p->raw;
+  const bool half = p->storage == FB_STORAGE_F16;
+  const AtmosphereParameters atm = convert(r);
+  const int trw = (int)r.transmittance_mu_size, trh = (int)r.transmittance_r_size;
+  const int irw = (int)r.irradiance_mu_s_size, irh = (int)r.irradiance_r_size;
+  const int scw = (int)(r.scattering_nu_size * r.scattering_mu_s_size), sch = (int)r.scattering_mu_size,
+            scd = (int)r.scattering_r_size;
+  const sampler2D s_tr = {tr, trw, trh}, s_dirr = {dirr, irw, irh};
+  const sampler3D s_dr = {dr, scw, sch, scd}, s_dm = {dm, scw, sch, scd};
+  const sampler3D s_dms = {dms, scw, sch, scd}, s_dens = {dens, scw, sch, scd};
+  long w = 0, h = 0;
+  void (*entry)(uvec3) = nullptr;
+  switch (pass) {
+    case 0:
+      p_transmittance::atmosphere = atm;
+      p_transmittance::table = image2D{tr, trw, trh, false};
+      entry = p_transmittance::main_entry;
+      w = trw; h = trh;
+      break;
+    case 1:
+      p_direct::atmosphere = atm;
+      p_direct::transmittance_texture = s_tr;
+      p_direct::delta_irradiance = image2D{dirr, irw, irh, false};
+      entry = p_direct::main_entry;
+      w = irw; h = irh;
+      break;
+    case 2:
+      p_single::atmosphere = atm;
+      p_single::transmittance = s_tr;
+      p_single::delta_rayleigh = image3D{dr, scw, sch, scd, half};
+      p_single::delta_mie = image3D{dm, scw, sch, scd, half};
+      p_single::scattering = image3D{sc, scw, sch, scd, half};
+      entry = p_single::main_entry;
+      w = scw; h = sch;
+      break;
+    case 3:
+      p_density::atmosphere = atm;
+      p_density::transmittance_texture = s_tr;
+      p_density::single_rayleigh_scattering_texture = s_dr;
+      p_density::single_mie_scattering_texture = s_dm;
+      p_density::multiple_scattering_texture = s_dms;
+      p_density::irradiance_texture = s_dirr;
+      p_density::scattering_density = image3D{dens, scw, sch, scd, half};
+      p_density::scattering_order = order;
+      entry = p_density::main_entry;
+      w = scw; h = sch;
+      break;
+    case 4:
+      p_indirect::atmosphere = atm;
+      p_indirect::single_rayleigh_scattering_texture = s_dr;
+      p_indirect::single_mie_scattering_texture = s_dm;
+      p_indirect::multiple_scattering_texture = s_dms;
+      p_indirect::delta_irradiance = image2D{dirr, irw, irh, false};
+      p_indirect::irradiance = image2D{ir, irw, irh, false};
+      p_indirect::scattering_order = order;
+      entry = p_indirect::main_entry;
+      w = irw; h = irh;
+      break;
+    case 5:
+      p_multiple::atmosphere = atm;
+      p_multiple::transmittance_texture = s_tr;
+      p_multiple::scattering_density_texture = s_dens;
+      p_multiple::delta_multiple_scattering = image3D{dms, scw, sch, scd, half};
+      p_multiple::scattering = image3D{sc, scw, sch, scd, half};
+      entry = p_multiple::main_entry;
+      w = scw; h = sch;
+      break;
+    default:
+      return FB_ERR_INVALID_ARGUMENT;
+  }
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int64_t k = 0; k < n; ++k) {
+    const int64_t id = ids[k];
+    entry(uvec3((uint)(id % w), (uint)((id / w) % h), (uint)(id / (w * h))));
+  }
+  return FB_OK;
+}
+
+}  // extern "C"

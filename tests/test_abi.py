@@ -98,3 +98,11 @@ def test_validate_accepts_benchmark_classes(native_lib):
 def test_status_strings(native_lib):
     assert native_lib.fb_status_string(0) == b"ok"
     assert native_lib.fb_abi_version() == 1
+
+
+def test_server_config_defaults(native_lib):
+    from fuzzyblue_gb300 import _native as N
+    c = N.c_server_config()
+    native_lib.fb_server_config_default(ctypes.byref(c))
+    assert c.hbm_budget_bytes == 120 << 30
+    assert c.max_batch >= 1 and c.max_inflight >= 1 and c.cache_entries >= 1
