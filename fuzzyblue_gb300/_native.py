@@ -82,6 +82,17 @@ class c_server_stats(ctypes.Structure):
     ]
 
 
+class c_tile_shape(ctypes.Structure):
+    _fields_ = [
+        ("density_columns", ctypes.c_uint32),
+        ("density_rows", ctypes.c_uint32),
+        ("density_variant", ctypes.c_uint32),
+        ("multiple_variant", ctypes.c_uint32),
+        ("density_ms", ctypes.c_float),
+        ("multiple_ms", ctypes.c_float),
+    ]
+
+
 class c_launch_profile(ctypes.Structure):
     _fields_ = [
         ("kernel", ctypes.c_uint32),
@@ -133,6 +144,10 @@ SIGNATURES = {
     "fb_atmosphere_destroy": (None, [_V]),
     "fb_batch_build": (_I, [_V, _V, _P, _U32, ctypes.POINTER(_V)]),
     "fb_builder_set_profiling": (_I, [_V, _I]),
+    "fb_builder_autotune": (_I, [_V, _P, _U32, _U32]),
+    "fb_builder_tuned_shape": (_I, [_V, _P, ctypes.POINTER(c_tile_shape)]),
+    "fb_builder_save_tuning": (_I, [_V, ctypes.c_char_p]),
+    "fb_builder_load_tuning": (_I, [_V, ctypes.c_char_p]),
     "fb_server_config_default": (None, [ctypes.POINTER(c_server_config)]),
     "fb_server_create": (_I, [_V, ctypes.POINTER(c_server_config), ctypes.POINTER(_V)]),
     "fb_server_submit": (_I, [_V, _P, ctypes.POINTER(_U64)]),

@@ -70,6 +70,27 @@ class Builder:
     def set_profiling(self, enabled: bool = True):
         N.check(N.lib().fb_builder_set_profiling(self._h, 1 if enabled else 0), "fb_builder_set_profiling")
 
+    def autotune(self, classes: Sequence[Parameters], batch: int = 8):
+        """Times every candidate tile shape and kernel variant of each class
+        (scattering sizes + precision) and keeps the fastest for later builds."""
+        arr = (c_params * len(classes))(*[p.to_c() for p in classes])
+        N.check(N.lib().fb_builder_autotune(self._h, arr, len(classes), batch), "fb_builder_autotune")
+
+    def tuned_shape(self, params: Parameters) -> Optional[dict]:
+        s = N.c_tile_shape()
+        c = params.to_c()
+        rc = N.lib().fb_builder_tuned_shape(self._h, ctypes.byref(c), ctypes.byref(s))
+        if rc == N.FB_ERR_NOT_FOUND:
+            return None
+        N.check(rc, "fb_builder_tuned_shape")
+        return {name: getattr(s, name) for name, _ in N.c_tile_shape._fields_}
+
+    def save_tuning(self, path: str):
+        N.check(N.lib().fb_builder_save_tuning(self._h, path.encode()), "fb_builder_save_tuning")
+
+    def load_tuning(self, path: str):
+        N.check(N.lib().fb_builder_load_tuning(self._h, path.encode()), "fb_builder_load_tuning")
+
     def set_allocator(self, alloc, release):
         """Routes the builder's device allocations through Python callables
         alloc(nbytes, stream) -> int pointer (0 = failure) and release(ptr, stream)."""

@@ -235,7 +235,7 @@ extern "C" int fb_builder_create(int device, fb_builder** out) {
   cudaDeviceProp prop;
   FB_CU(cudaGetDeviceProperties(&prop, device));
   cudaFuncAttributes fa;
-  if (cudaFuncGetAttributes(&fa, fb::kernel_plain(fb::kPassDensity, 1)) != cudaSuccess) {
+  if (cudaFuncGetAttributes(&fa, fb::kernel_plain(fb::kPassDensity, 1, 0)) != cudaSuccess) {
     cudaGetLastError();
     return fail(FB_ERR_NO_KERNEL, "no sm_103a kernel image loads on device %d (%s, sm_%d%d)", device, prop.name,
                 prop.major, prop.minor);
@@ -265,8 +265,9 @@ extern "C" int fb_builder_create(int device, fb_builder** out) {
   }
   for (int mode = 0; mode < 2; ++mode)
     for (int pass = 0; pass < 4; ++pass)
-      for (int tpt : {1, 2, 4, 8}) {
-        const void* k = fb::kernel_for(mode == 1, pass, tpt);
+      for (int tpt : {1, 2, 4, 8})
+        for (int variant : {0, 1}) {
+        const void* k = fb::kernel_for(mode == 1, pass, tpt, variant);
         cudaFuncAttributes kfa;
         if (cudaFuncGetAttributes(&kfa, k) != cudaSuccess ||
             cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -432,6 +433,7 @@ struct PlannedLaunch {
   int pass;
   bool mixed;
   int tpt;
+  int variant;
   int order;
   int nseg;
   int seg_njobs[2];
@@ -460,7 +462,26 @@ void add_segment(Plan& P, PlannedLaunch& L, int s, const std::vector<int>& jobs,
   L.seg_total[s] = acc;
 }
 
-void plan_group(Plan& P, const std::vector<DevAtmo>& A, const std::vector<int>& group, bool mixed) {
+// Occupancy variant of a launch: the tuned variant of its largest atmosphere.
+int launch_variant(const std::vector<DevAtmo>& A, const std::vector<int>& jobs, const fbi::Tuning& tun, bool mixed,
+                   bool density) {
+  int best = -1;
+  size_t best_n = 0;
+  for (int j : jobs) {
+    const size_t n = (size_t)A[j].W * A[j].sc_mu * A[j].sc_r;
+    if (best < 0 || n > best_n) {
+      best = j;
+      best_n = n;
+    }
+  }
+  if (best < 0) return 0;
+  const DevAtmo& a = A[best];
+  const fbi::TuneEntry* e = fbi::tuning_find(tun, a.sc_r, a.sc_mu, a.sc_mus, a.sc_nu, mixed ? 1 : 0);
+  return e ? (density ? e->dens_variant : e->ms_variant) : 0;
+}
+
+void plan_group(Plan& P, const std::vector<DevAtmo>& A, const std::vector<int>& group, bool mixed,
+                const fbi::Tuning& tun) {
   if (group.empty()) return;
   int max_order = 1;
   for (int j : group) max_order = std::max(max_order, A[j].order);
@@ -516,6 +537,7 @@ void plan_group(Plan& P, const std::vector<DevAtmo>& A, const std::vector<int>& 
     add_segment(P, D, 0, jobs, t0);
     add_segment(P, D, 1, jobs, t1);
     D.nseg = 2;
+    D.variant = launch_variant(A, jobs, tun, mixed, true);
     P.launches.push_back(D);
     PlannedLaunch M = mk(fb::kPassMultiple, n);
     std::vector<int> tm;
@@ -528,6 +550,7 @@ void plan_group(Plan& P, const std::vector<DevAtmo>& A, const std::vector<int>& 
     }
     add_segment(P, M, 0, jobs, tm);
     M.nseg = 1;
+    M.variant = launch_variant(A, jobs, tun, mixed, false);
     P.launches.push_back(M);
   }
 }
@@ -571,7 +594,9 @@ void fill_devatmo(DevAtmo& d, const fb_params& p, const fbi::Tuning& tun) {
   d.order = (int)p.order;
   d.f16 = p.storage == FB_STORAGE_F16;
   d.W = d.sc_nu * d.sc_mus;
-  fbi::tuning_density_shape(tun, d.sc_r, d.sc_mu, d.sc_mus, d.sc_nu, &d.dens_S, &d.dens_chunk);
+  const fbi::TuneEntry* te = fbi::tuning_find(tun, d.sc_r, d.sc_mu, d.sc_mus, d.sc_nu, (int)p.precision);
+  d.dens_S = te ? te->dens_S : 0;
+  d.dens_chunk = te ? te->dens_chunk : 0;
 }
 
 }  // namespace
@@ -655,8 +680,8 @@ int build(fb_builder* b, cudaStream_t s, const fb_params* params, uint32_t count
   Plan plan;
   std::vector<int> g_plain, g_mixed;
   for (uint32_t i = 0; i < count; ++i) (params[i].precision == FB_PRECISION_MIXED ? g_mixed : g_plain).push_back((int)i);
-  plan_group(plan, P->dev, g_plain, false);
-  plan_group(plan, P->dev, g_mixed, true);
+  plan_group(plan, P->dev, g_plain, false, tun);
+  plan_group(plan, P->dev, g_mixed, true, tun);
   const size_t atm_bytes = align256(sizeof(DevAtmo) * count);
   const size_t int_bytes = align256(sizeof(int) * std::max<size_t>(plan.ints.size(), 1));
   const size_t cnt_bytes = align256(sizeof(unsigned) * plan.launches.size());
@@ -683,7 +708,7 @@ int build(fb_builder* b, cudaStream_t s, const fb_params* params, uint32_t count
   for (size_t li = 0; li < plan.launches.size(); ++li) {
     const PlannedLaunch& L = plan.launches[li];
     Ready R;
-    R.fn = fb::kernel_for(L.mixed, L.pass, L.tpt);
+    R.fn = fb::kernel_for(L.mixed, L.pass, L.tpt, L.variant);
     R.smem = L.smem;
     cudaFuncAttributes kfa;
     if (cudaFuncGetAttributes(&kfa, R.fn) != cudaSuccess) return bail(FB_ERR_CUDA, "cudaFuncGetAttributes failed");

@@ -385,6 +385,86 @@ struct Geo64 {
   }
 };
 
+// The MIXED geometry used per trapezoid sample: FP64 only where cancellation
+// happens (the sample state q, s; the ground discriminant s^2 - q; T^2 - r^2),
+// every later step in FP32 on quantities that no longer cancel. Same results
+// as Geo64 to FP32 precision, at a fraction of its FP64 instructions (FP64
+// issues at 1/64 of the FP32 rate on this part).
+struct GeoMx {
+  float R, T, H, H2f, inv_H, trm1, trr1, scr1, M1f, Mf;
+  double H2;
+  __device__ __forceinline__ void init(const DevAtmo& a) {
+    R = a.bottom;
+    T = a.top;
+    H2 = (double)a.top * a.top - (double)a.bottom * a.bottom;
+    H2f = (float)H2;
+    H = (float)sqrt(H2);
+    inv_H = (float)(1.0 / sqrt(H2));
+    trm1 = float(a.tr_mu - 1);
+    trr1 = float(a.tr_r - 1);
+    scr1 = float(a.sc_r - 1);
+    Mf = float(a.sc_mu / 2);
+    M1f = float(a.sc_mu / 2 - 1);
+  }
+  // distance to the top from (q, s): e = T^2 - r^2 in FP64, the rest in FP32
+  __device__ __forceinline__ float dist_top(double q, double s, float& e_out) const {
+    const double e = H2 - q;
+    const float root = sqrtf((float)fmax(fma(s, s, e), 0.0));
+    const float ef = (float)e, sf = (float)s;
+    e_out = ef;
+    return fmaxf(sf > 0.0f ? __fdividef(ef, sf + root) : root - sf, 0.0f);
+  }
+  __device__ __forceinline__ void tr_texel(double q, double s, float& tx, float& ty) const {
+    const float qf = fmaxf((float)q, 0.0f);
+    const float rho = sqrtf(qf), r = sqrtf(qf + R * R);
+    float e;
+    const float d = dist_top(q, s, e);
+    const float d_min = __fdividef(e, T + r);
+    tx = __fdividef(d - d_min, rho + H - d_min) * trm1;
+    ty = rho * inv_H * trr1;
+  }
+  __device__ __forceinline__ float3 tr_to_top(const DevAtmo& a, double q, double s) const {
+    float tx, ty;
+    tr_texel(q, s, tx, ty);
+    return fetch2(a.tr, a.tr_mu, axis_texel(tx, a.tr_mu), axis_texel(ty, a.tr_r));
+  }
+  __device__ __forceinline__ float3 tr_segment(const DevAtmo& a, double q, double s, double d, bool ground) const {
+    double qd = fma(d, 2.0 * s + d, q), sd = s + d;
+    qd = fmin(fmax(qd, 0.0), H2);
+    const double rd = (double)sqrtf((float)qd + R * R);
+    sd = fmin(fmax(sd, -rd), rd);
+    float3 num, den;
+    if (ground) {
+      num = tr_to_top(a, qd, -sd);
+      den = tr_to_top(a, q, -s);
+    } else {
+      num = tr_to_top(a, q, s);
+      den = tr_to_top(a, qd, sd);
+    }
+    return min1(num / den);
+  }
+  __device__ __forceinline__ float sc_r_texel(double q) const {
+    return sqrtf(fmaxf((float)q, 0.0f)) * inv_H * scr1;
+  }
+  // scattering.h:23-46 as a texel coordinate along mu
+  __device__ __forceinline__ float sc_mu_texel(double q, double s, bool ground) const {
+    const float qf = fmaxf((float)q, 0.0f);
+    const float rho = sqrtf(qf), r = sqrtf(qf + R * R), sf = (float)s;
+    if (ground) {
+      const float root = sqrtf((float)fmax(fma(s, s, -q), 0.0));  // s^2 - q in FP64
+      const float d = sf < 0.0f ? __fdividef(qf, root - sf) : fmaxf(-sf - root, 0.0f);
+      const float d_min = __fdividef(qf, r + R);
+      const float x = rho == d_min ? 0.0f : __fdividef(d - d_min, rho - d_min);
+      return M1f * (1.0f - x);
+    }
+    float e;
+    const float d = dist_top(q, s, e);
+    const float d_min = __fdividef(e, T + r);
+    const float x = __fdividef(d - d_min, rho + H - d_min);
+    return fmaf(x, M1f, Mf);
+  }
+};
+
 // FP32 form of Geo64::mus_unit for per-texel-sample use in the mixed mode: the
 // same cancellation-free distance, single precision, constants precomputed.
 struct MuS32 {

@@ -19,15 +19,18 @@ TableSizes sizes_of(const fb_params& p);
 // Tile shapes per scattering-table class, chosen by the autotuner
 // (fb_builder_autotune) or by the default rule.
 struct TuneEntry {
-  int sc_r, sc_mu, sc_mus, sc_nu;
+  int sc_r, sc_mu, sc_mus, sc_nu, precision;
   int dens_S, dens_chunk;  // scattering-density tile: mu_s columns x mu rows
+  int dens_variant, ms_variant;
+  float dens_ms, ms_ms;
 };
 struct Tuning {
   std::vector<TuneEntry> entries;
 };
 void tuning_load_default(Tuning& t);
-// Tile shape of a table class (0, 0 when the class is not tuned: default rule).
-void tuning_density_shape(const Tuning& t, int sc_r, int sc_mu, int sc_mus, int sc_nu, int* S, int* chunk);
+// The entry of a class, or nullptr (default rule, variants 0).
+const TuneEntry* tuning_find(const Tuning& t, int sc_r, int sc_mu, int sc_mus, int sc_nu, int precision);
+void tuning_set(Tuning& t, const TuneEntry& e);
 
 void builder_ref(fb_builder* b);
 void builder_unref(fb_builder* b);

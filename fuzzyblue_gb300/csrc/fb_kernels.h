@@ -8,13 +8,14 @@ namespace fb {
 
 enum PassKind { kPassTransmittance = 0, kPassSingle = 1, kPassDensity = 2, kPassMultiple = 3 };
 
-// Kernel of (mode, pass, texels-per-thread); tpt is used by kPassMultiple only
-// (1, 2, 4 or 8).
-const void* kernel_plain(int pass, int tpt);
-const void* kernel_mixed(int pass, int tpt);
+// Kernel of (mode, pass, texels-per-thread, occupancy variant); tpt is used by
+// kPassMultiple only (1, 2, 4 or 8); variant (0 or 1) by the density and
+// multiple-scattering passes.
+const void* kernel_plain(int pass, int tpt, int variant);
+const void* kernel_mixed(int pass, int tpt, int variant);
 
-inline const void* kernel_for(bool mixed, int pass, int tpt) {
-  return mixed ? kernel_mixed(pass, tpt) : kernel_plain(pass, tpt);
+inline const void* kernel_for(bool mixed, int pass, int tpt, int variant = 0) {
+  return mixed ? kernel_mixed(pass, tpt, variant) : kernel_plain(pass, tpt, variant);
 }
 
 inline int tpt_for_width(int W) {

@@ -7,23 +7,29 @@ namespace fb {
 
 template __global__ void k_transmittance<false>(LaunchArgs);
 template __global__ void k_single<false>(LaunchArgs);
-template __global__ void k_density<false>(LaunchArgs);
-template __global__ void k_multiple<false, 1>(LaunchArgs);
-template __global__ void k_multiple<false, 2>(LaunchArgs);
-template __global__ void k_multiple<false, 4>(LaunchArgs);
-template __global__ void k_multiple<false, 8>(LaunchArgs);
+template __global__ void k_density<false, 0>(LaunchArgs);
+template __global__ void k_density<false, 1>(LaunchArgs);
+template __global__ void k_multiple<false, 1, 0>(LaunchArgs);
+template __global__ void k_multiple<false, 2, 0>(LaunchArgs);
+template __global__ void k_multiple<false, 4, 0>(LaunchArgs);
+template __global__ void k_multiple<false, 8, 0>(LaunchArgs);
+template __global__ void k_multiple<false, 1, 1>(LaunchArgs);
+template __global__ void k_multiple<false, 2, 1>(LaunchArgs);
+template __global__ void k_multiple<false, 4, 1>(LaunchArgs);
+template __global__ void k_multiple<false, 8, 1>(LaunchArgs);
 
-const void* kernel_plain(int pass, int tpt) {
+const void* kernel_plain(int pass, int tpt, int variant) {
+  const bool v1 = variant == 1;
   switch (pass) {
     case kPassTransmittance: return (const void*)k_transmittance<false>;
     case kPassSingle: return (const void*)k_single<false>;
-    case kPassDensity: return (const void*)k_density<false>;
+    case kPassDensity: return v1 ? (const void*)k_density<false, 1> : (const void*)k_density<false, 0>;
     case kPassMultiple:
       switch (tpt) {
-        case 1: return (const void*)k_multiple<false, 1>;
-        case 2: return (const void*)k_multiple<false, 2>;
-        case 4: return (const void*)k_multiple<false, 4>;
-        default: return (const void*)k_multiple<false, 8>;
+        case 1: return v1 ? (const void*)k_multiple<false, 1, 1> : (const void*)k_multiple<false, 1, 0>;
+        case 2: return v1 ? (const void*)k_multiple<false, 2, 1> : (const void*)k_multiple<false, 2, 0>;
+        case 4: return v1 ? (const void*)k_multiple<false, 4, 1> : (const void*)k_multiple<false, 4, 0>;
+        default: return v1 ? (const void*)k_multiple<false, 8, 1> : (const void*)k_multiple<false, 8, 0>;
       }
   }
   return nullptr;

@@ -357,30 +357,31 @@ __device__ void tile_single(const DevAtmo& a, int tile, unsigned char* smem) {
       o.y1 = ay.i1;
       o.fy = ay.f;
     } else {
-      Geo64 G;
+      GeoMx G;
       G.init(a);
-      double d = double(i) * ri.dxd;
-      double q = ri.q + d * (2.0 * ri.s + d), s = ri.s + d;
-      G.clamp_point(q, s);
-      double r_d = G.radius(q);
+      const double d = double(i) * ri.dxd;
+      double q = fma(d, 2.0 * ri.s + d, ri.q);
+      q = fmin(fmax(q, 0.0), G.H2);
+      const float qf = (float)q;
+      const float r_d = sqrtf(qf + G.R * G.R);
       tv = G.tr_segment(a, ri.q, ri.s, d, ri.ground);
       o.d = (float)d;
-      o.r_d = (float)r_d;
+      o.r_d = r_d;
       o.rr_d = 0.f;
-      float h = (float)(q / (r_d + G.R));
+      const float h = __fdividef(qf, r_d + G.R);
       o.rho_r = profile_density(a.ray_d, h);
       o.rho_m = profile_density(a.mie_d, h);
-      double rho = sqrt(q);
-      o.cos_h = (float)(-rho / r_d);
-      double sin_h = G.R / r_d;
-      o.lo = (float)(-sin_h * a.sun_radius);
-      o.inv_w = (float)(1.0 / (2.0 * sin_h * a.sun_radius));
-      o.inv_r = (float)(1.0 / r_d);
+      const float rho = sqrtf(qf);
+      o.inv_r = 1.0f / r_d;
+      o.cos_h = -rho * o.inv_r;
+      const float sin_h = G.R * o.inv_r;
+      o.lo = -sin_h * a.sun_radius;
+      o.inv_w = 1.0f / (2.0f * sin_h * a.sun_radius);
       o.e = (float)(G.H2 - q);  // T^2 - r_d^2
-      const double dmin = (G.H2 - q) / (G.T + r_d);
-      o.dmin = (float)dmin;
-      o.inv_span = (float)(1.0 / (rho + G.H - dmin));
-      const Axis ay = axis_texel(rho / G.H * double(a.tr_r - 1), a.tr_r);
+      const float dmin = __fdividef(o.e, G.T + r_d);
+      o.dmin = dmin;
+      o.inv_span = 1.0f / (rho + G.H - dmin);
+      const Axis ay = axis_texel(rho * G.inv_H * G.trr1, a.tr_r);
       o.y0 = ay.i0;
       o.y1 = ay.i1;
       o.fy = ay.f;
@@ -531,7 +532,7 @@ struct DensLayout {
   double* col_musd; // S (MIXED)
   double2* ymu;     // chunk (MIXED): (mu, 1 - mu^2)
   double* nuraw;    // sc_nu (MIXED)
-  double* acc;      // kDensThreads * kDensMaxGroup * 3 (MIXED: FP64 sum over theta rows)
+  float* acc;       // kDensThreads * kDensMaxGroup * 3 * 2 (MIXED: Kahan sum over theta rows)
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
@@ -551,7 +552,7 @@ __host__ __device__ inline size_t dens_layout(unsigned char* base, int dens_n, i
   size_t o_irow = take(sizeof(float4) * ir_mus);
   size_t o_cm = take(sizeof(float) * S), o_cmd = take(sizeof(double) * S);
   size_t o_ymu = take(mixed ? sizeof(double2) * chunk : 0), o_nu = take(mixed ? sizeof(double) * sc_nu : 0);
-  size_t o_acc = take(mixed ? sizeof(double) * kDensThreads * kDensMaxGroup * 3 : 0);
+  size_t o_acc = take(mixed ? sizeof(float) * kDensThreads * kDensMaxGroup * 6 : 0);
   if (L) {
     L->th = (DensTheta*)(base + o_th);
     L->tay = (Axis*)(base + o_tay);
@@ -564,7 +565,7 @@ __host__ __device__ inline size_t dens_layout(unsigned char* base, int dens_n, i
     L->col_musd = (double*)(base + o_cmd);
     L->ymu = (double2*)(base + o_ymu);
     L->nuraw = (double*)(base + o_nu);
-    L->acc = (double*)(base + o_acc);
+    L->acc = (float*)(base + o_acc);
   }
   return o;
 }
@@ -758,8 +759,26 @@ __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned cha
   const bool active = tid < sh.S * per_s && cl < ns && yl < ny;
   if (active) {
     const int G = sh.G, y = y0 + yl, si = s0 + cl;
-    float mu, ox, mu_s;
+    float mu = 0.f, ox = 0.f, mu_s;
     float sx[kDensMaxGroup], sy[kDensMaxGroup];
+    // MIXED: the texel frame in FP64 (scattering.h:134-136 clamp, frame of
+    // scattering_density.comp:28-32): sq, mu mu_s and 1/(1-mu^2) are shared by
+    // the group; per texel delta = nu - mu mu_s in [-sq, sq] and
+    // sun_y^2 = (sq - delta)(sq + delta) / (1 - mu^2), exactly 0 in the plane.
+    double mx_sq = 0.0, mx_mm = 0.0, mx_iom = 0.0, mx_isom = 0.0, mx_omus = 0.0;
+    bool mx_pole = false;
+    if (MX) {
+      const double2 ym = S.ymu[yl];
+      const double musd = S.col_musd[cl];
+      mx_omus = (1.0 - musd) * (1.0 + musd);
+      mx_sq = sqrt(ym.y * mx_omus);
+      mx_mm = ym.x * musd;
+      mx_pole = ym.y == 0.0;
+      mx_iom = mx_pole ? 0.0 : 1.0 / ym.y;
+      mx_isom = mx_pole ? 0.0 : 1.0 / sqrt(ym.y);
+      mu = (float)ym.x;
+      ox = (float)sqrt(ym.y);
+    }
 #pragma unroll
     for (int j = 0; j < kDensMaxGroup; ++j) {
       sx[j] = sy[j] = 0.f;
@@ -776,23 +795,14 @@ __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned cha
           sx[j] = ox == 0.0f ? 0.0f : (nu - mu * ms) / ox;
           sy[j] = sqrtf(gmax(1.0f - sx[j] * sx[j] - ms * ms, 0.0f));
         } else {
-          // the same frame in FP64, nu clamped (scattering.h:134-136) as
-          // delta = nu - mu mu_s in [-sq, sq]; sun_y^2 = (sq - delta)(sq + delta)
-          // / (1 - mu^2) is exactly 0 when the sun lies in the view plane
-          const double2 ym = S.ymu[yl];
-          const double mud = ym.x, om = ym.y, musd = S.col_musd[cl];
-          const double omus = (1.0 - musd) * (1.0 + musd);
-          const double sq = sqrt(om * omus), mm = mud * musd;
-          const double delta = gclamp(S.nuraw[nu_i] - mm, -sq, sq);
-          if (om == 0.0) {
+          const double delta = gclamp(S.nuraw[nu_i] - mx_mm, -mx_sq, mx_sq);
+          if (mx_pole) {
             sx[j] = 0.f;
-            sy[j] = (float)sqrt(gmax(omus, 0.0));
+            sy[j] = sqrtf((float)mx_omus);
           } else {
-            sx[j] = (float)(delta / sqrt(om));
-            sy[j] = (float)sqrt(gmax((sq - delta) * (sq + delta), 0.0) / om);
+            sx[j] = (float)(delta * mx_isom);
+            sy[j] = sqrtf((float)fmax((mx_sq - delta) * (mx_sq + delta) * mx_iom, 0.0));
           }
-          mu = (float)mud;
-          ox = (float)sqrt(om);
         }
       }
     }
@@ -814,9 +824,9 @@ __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned cha
     float3 acc[kDensMaxGroup];
 #pragma unroll
     for (int j = 0; j < kDensMaxGroup; ++j) acc[j] = make_float3(0.f, 0.f, 0.f);
-    double* accd = S.acc + (size_t)tid * kDensMaxGroup * 3;
+    float* accs = S.acc + (size_t)tid * kDensMaxGroup * 6;  // (sum, compensation) x 3 x G
     if (MX) {
-      for (int j = 0; j < 3 * kDensMaxGroup; ++j) accd[j] = 0.0;
+      for (int j = 0; j < 6 * kDensMaxGroup; ++j) accs[j] = 0.f;
     }
     const size_t ptab = 2 * (size_t)sh.S * NT * NK;
     for (int l = 0; l < NT; ++l) {
@@ -875,13 +885,13 @@ __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned cha
         }
       }
       if (MX) {
-        // FP64 sum over theta rows of the FP32 sums over one row
+        // Kahan sum over theta rows of the FP32 sums over one row
 #pragma unroll
         for (int j = 0; j < kDensMaxGroup; ++j) {
           if (j < G) {
-            accd[3 * j] += acc[j].x;
-            accd[3 * j + 1] += acc[j].y;
-            accd[3 * j + 2] += acc[j].z;
+            Kahan3::add1(accs[6 * j], accs[6 * j + 3], acc[j].x);
+            Kahan3::add1(accs[6 * j + 1], accs[6 * j + 4], acc[j].y);
+            Kahan3::add1(accs[6 * j + 2], accs[6 * j + 5], acc[j].z);
             acc[j] = make_float3(0.f, 0.f, 0.f);
           }
         }
@@ -893,7 +903,9 @@ __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned cha
         const int x = (grp * G + j) * a.sc_mus + si;
         const size_t tt = ((size_t)zi * a.sc_mu + y) * a.W + x;
         float3 o = acc[j];
-        if (MX) o = make_float3((float)accd[3 * j], (float)accd[3 * j + 1], (float)accd[3 * j + 2]);
+        if (MX)
+          o = make_float3(accs[6 * j] - accs[6 * j + 3], accs[6 * j + 1] - accs[6 * j + 4],
+                          accs[6 * j + 2] - accs[6 * j + 5]);
         a.dens[tt] = store_round4(make_float4(o.x, o.y, o.z, 0.f), a.f16);
       }
     }
@@ -1049,7 +1061,9 @@ __device__ void tile_indirect(const DevAtmo& a, int order, int tile, unsigned ch
   }
 }
 
-template <bool MX> __global__ void __launch_bounds__(kDensThreads, 4) k_density(LaunchArgs L) {
+// V selects the occupancy variant chosen by the autotuner: V = 0 caps the
+// registers for 4 resident blocks per SM, V = 1 for 6.
+template <bool MX, int V> __global__ void __launch_bounds__(kDensThreads, V == 0 ? 4 : 6) k_density(LaunchArgs L) {
   extern __shared__ __align__(16) unsigned char smem[];
   int seg, job, tile;
   while (next_item(L, seg, job, tile)) {
@@ -1115,16 +1129,18 @@ __device__ void tile_multiple(const DevAtmo& a, int tile, unsigned char* smem) {
       o.d = d;
       o.inv_r = 1.0f / r_i;
     } else {
-      Geo64 G;
+      GeoMx G;
       G.init(a);
       const double d = double(i) * ri.dxd;
-      double q = ri.q + d * (2.0 * ri.s + d), s = ri.s + d;
-      G.clamp_point(q, s);
+      double q = fma(d, 2.0 * ri.s + d, ri.q), s = ri.s + d;
+      q = fmin(fmax(q, 0.0), G.H2);
+      const float r_i = sqrtf((float)q + G.R * G.R);
+      s = fmin(fmax(s, -(double)r_i), (double)r_i);
       tv = G.tr_segment(a, ri.q, ri.s, d, ri.ground);
-      az = axis_texel(G.sc_r_texel(a, q), a.sc_r);
-      ay = axis_texel(G.sc_mu_texel(a, q, s, ri.ground), a.sc_mu);
+      az = axis_texel(G.sc_r_texel(q), a.sc_r);
+      ay = axis_texel(G.sc_mu_texel(q, s, ri.ground), a.sc_mu);
       o.d = (float)d;
-      o.inv_r = (float)(1.0 / G.radius(q));
+      o.inv_r = 1.0f / r_i;
     }
     o.wdx = ri.dx * w;
     o.tvx = tv.x;
@@ -1165,30 +1181,51 @@ __device__ void tile_multiple(const DevAtmo& a, int tile, unsigned char* smem) {
   }
   const float4* dens = a.dens;
   const size_t plane = (size_t)a.sc_mu * W;
-  auto build = [&](int i, float4* dst) {
-    for (int k = tid; k < slab_n; k += kThreads) {
-      const int lr = k / W, x = k % W;
-      const MSRec& o = rec[lr * NS + i];
-      const float4 a00 = ld4(dens + o.z0 * plane + (size_t)o.y0 * W + x);
-      const float4 a10 = ld4(dens + o.z0 * plane + (size_t)o.y1 * W + x);
-      const float4 a01 = ld4(dens + o.z1 * plane + (size_t)o.y0 * W + x);
-      const float4 a11 = ld4(dens + o.z1 * plane + (size_t)o.y1 * W + x);
-      const float w00 = (1.f - o.fy) * (1.f - o.fz), w10 = o.fy * (1.f - o.fz);
-      const float w01 = (1.f - o.fy) * o.fz, w11 = o.fy * o.fz;
-      float4 v;
-      v.x = fmaf(w11, a11.x, fmaf(w01, a01.x, fmaf(w10, a10.x, w00 * a00.x)));
-      v.y = fmaf(w11, a11.y, fmaf(w01, a01.y, fmaf(w10, a10.y, w00 * a00.y)));
-      v.z = fmaf(w11, a11.z, fmaf(w01, a01.z, fmaf(w10, a10.z, w00 * a00.z)));
-      v.w = 0.f;
-      dst[k] = v;
+  // Slab of sample i: the density table interpolated in (mu, r) at the
+  // sample, for every x of the row.
+  float4 nx[TPT][4];
+  auto load = [&](int i) {
+#pragma unroll
+    for (int j = 0; j < TPT; ++j) {
+      const int k = tid + j * kThreads;
+      if (k < slab_n) {
+        const int lr = k / W, x = k % W;
+        const MSRec& o = rec[lr * NS + i];
+        nx[j][0] = ld4(dens + o.z0 * plane + (size_t)o.y0 * W + x);
+        nx[j][1] = ld4(dens + o.z0 * plane + (size_t)o.y1 * W + x);
+        nx[j][2] = ld4(dens + o.z1 * plane + (size_t)o.y0 * W + x);
+        nx[j][3] = ld4(dens + o.z1 * plane + (size_t)o.y1 * W + x);
+      }
     }
   };
-  build(0, slab);
+  auto store = [&](int i, float4* dst) {
+#pragma unroll
+    for (int j = 0; j < TPT; ++j) {
+      const int k = tid + j * kThreads;
+      if (k < slab_n) {
+        const MSRec& o = rec[(k / W) * NS + i];
+        const float w00 = (1.f - o.fy) * (1.f - o.fz), w10 = o.fy * (1.f - o.fz);
+        const float w01 = (1.f - o.fy) * o.fz, w11 = o.fy * o.fz;
+        const float4 a00 = nx[j][0], a10 = nx[j][1], a01 = nx[j][2], a11 = nx[j][3];
+        float4 v;
+        v.x = fmaf(w11, a11.x, fmaf(w01, a01.x, fmaf(w10, a10.x, w00 * a00.x)));
+        v.y = fmaf(w11, a11.y, fmaf(w01, a01.y, fmaf(w10, a10.y, w00 * a00.y)));
+        v.z = fmaf(w11, a11.z, fmaf(w01, a01.z, fmaf(w10, a10.z, w00 * a00.z)));
+        v.w = 0.f;
+        dst[k] = v;
+      }
+    }
+  };
+  load(0);
+  store(0, slab);
   __syncthreads();
   const float fmus = float(a.sc_mus);
   for (int i = 0; i < NS; ++i) {
     const float4* cur = slab + (i & 1) * slab_stride;
-    if (i + 1 < NS) build(i + 1, slab + ((i + 1) & 1) * slab_stride);
+    // the next sample's rows load after this sample's arithmetic: holding them
+    // across it costs more occupancy than the overlap gains
+    constexpr bool kPrefetch = false;
+    if (kPrefetch && i + 1 < NS) load(i + 1);
 #pragma unroll
     for (int j = 0; j < TPT; ++j) {
       const int k = tid + j * kThreads;
@@ -1196,7 +1233,6 @@ __device__ void tile_multiple(const DevAtmo& a, int tile, unsigned char* smem) {
         const int lr = k / W;
         const MSRec& o = rec[lr * NS + i];
         const float nu = c_nu[j];
-        // multiple_scattering.comp:38 and scattering.h:48-56
         const float tx = c_tex[j];
         Axis x0, x1;
         if (!MX) {
@@ -1224,6 +1260,10 @@ __device__ void tile_multiple(const DevAtmo& a, int tile, unsigned char* smem) {
         else acc[j].add(v);
       }
     }
+    if (i + 1 < NS) {
+      if (!kPrefetch) load(i + 1);
+      store(i + 1, slab + ((i + 1) & 1) * slab_stride);
+    }
     __syncthreads();
   }
   // outputs: delta multiple scattering and the final table (:91-92)
@@ -1242,16 +1282,20 @@ __device__ void tile_multiple(const DevAtmo& a, int tile, unsigned char* smem) {
                                a.f16);
       } else {
         double* s3 = a.sc_acc + 3 * t;
-        s3[0] += (double)ms.x / pr;
-        s3[1] += (double)ms.y / pr;
-        s3[2] += (double)ms.z / pr;
+        const float ipr = 1.0f / pr;
+        s3[0] += (double)(ms.x * ipr);
+        s3[1] += (double)(ms.y * ipr);
+        s3[2] += (double)(ms.z * ipr);
         a.sc[t] = store_round4(make_float4((float)s3[0], (float)s3[1], (float)s3[2], old.w), a.f16);
       }
     }
   }
 }
 
-template <bool MX, int TPT> __global__ void __launch_bounds__(kThreads) k_multiple(LaunchArgs L) {
+// V = 0: registers capped for 4 resident blocks per SM (2 for wide rows);
+// V = 1: for 3 (1 for wide rows).
+template <bool MX, int TPT, int V>
+__global__ void __launch_bounds__(kThreads, TPT <= 2 ? (V == 0 ? 4 : 3) : (V == 0 ? 2 : 1)) k_multiple(LaunchArgs L) {
   extern __shared__ __align__(16) unsigned char smem[];
   int seg, job, tile;
   while (next_item(L, seg, job, tile)) tile_multiple<MX, TPT>(L.atm[job], tile, smem);

@@ -62,7 +62,8 @@ struct Batch {
   int stream_slot = -1;
   std::vector<Entry*> entries;
   size_t bytes = 0;
-  std::atomic<bool> done{false};
+  bool has_callback = false;      // completion is signalled by the host callback
+  std::atomic<bool> done{false};  // set by that callback as its last action
 };
 
 // Cache key: the parameter bytes with every padding and reserved field zeroed.
@@ -146,18 +147,27 @@ void evict(fb_server* s, size_t need, bool for_count) {
   }
 }
 
+// Runs on a CUDA driver thread when the batch's stream reaches it. The batch
+// (and with it the server) stays alive until `done` is set, so storing it is
+// the callback's last access to either.
 void CUDART_CB on_batch_done(void* arg) {
   auto* pair = static_cast<std::pair<fb_server*, Batch*>*>(arg);
-  pair->second->done.store(true);
-  pair->first->cv.notify_all();
+  fb_server* s = pair->first;
+  Batch* bt = pair->second;
   delete pair;
+  s->cv.notify_all();
+  bt->done.store(true);
 }
 
 void collect(fb_server* s) {
   for (size_t i = 0; i < s->inflight.size();) {
     Batch* bt = s->inflight[i];
-    if (!bt->done.load() && cudaEventQuery(fbi::pending_event(bt->pending)) != cudaSuccess) {
-      cudaGetLastError();
+    bool finished = bt->done.load();
+    if (!bt->has_callback && !finished) {
+      finished = cudaEventQuery(fbi::pending_event(bt->pending)) == cudaSuccess;
+      if (!finished) cudaGetLastError();
+    }
+    if (!finished) {
       ++i;
       continue;
     }
@@ -251,7 +261,9 @@ void admit(fb_server* s) {
     s->st.batches++;
     s->batched_atmospheres += (double)params.size();
     auto* arg = new std::pair<fb_server*, Batch*>(s, bt);
-    if (cudaLaunchHostFunc(s->streams[slot], on_batch_done, arg) != cudaSuccess) {
+    if (cudaLaunchHostFunc(s->streams[slot], on_batch_done, arg) == cudaSuccess) {
+      bt->has_callback = true;
+    } else {
       cudaGetLastError();
       delete arg;  // completion is then found by polling the batch's event
     }

@@ -33,15 +33,21 @@ cudaError_t launch_to_half(const float4* src, void* dst, size_t n, cudaStream_t 
 
 void tuning_load_default(Tuning& t) { t.entries.clear(); }
 
-void tuning_density_shape(const Tuning& t, int sc_r, int sc_mu, int sc_mus, int sc_nu, int* S, int* chunk) {
-  *S = 0;
-  *chunk = 0;
+const TuneEntry* tuning_find(const Tuning& t, int sc_r, int sc_mu, int sc_mus, int sc_nu, int precision) {
   for (const TuneEntry& e : t.entries)
-    if (e.sc_r == sc_r && e.sc_mu == sc_mu && e.sc_mus == sc_mus && e.sc_nu == sc_nu) {
-      *S = e.dens_S;
-      *chunk = e.dens_chunk;
+    if (e.sc_r == sc_r && e.sc_mu == sc_mu && e.sc_mus == sc_mus && e.sc_nu == sc_nu && e.precision == precision)
+      return &e;
+  return nullptr;
+}
+
+void tuning_set(Tuning& t, const TuneEntry& e) {
+  for (TuneEntry& x : t.entries)
+    if (x.sc_r == e.sc_r && x.sc_mu == e.sc_mu && x.sc_mus == e.sc_mus && x.sc_nu == e.sc_nu &&
+        x.precision == e.precision) {
+      x = e;
       return;
     }
+  t.entries.push_back(e);
 }
 
 }  // namespace fbi

@@ -259,6 +259,31 @@ void fb_atmosphere_destroy(fb_atmosphere* a);
 int fb_batch_build(fb_builder* b, void* stream, const fb_params* params,
                    uint32_t count, fb_pending** out);
 
+/* ---- tile-shape autotuning ----------------------------------------------- */
+
+/* The tuned launch shapes of one table class (scattering sizes + precision). */
+typedef struct fb_tile_shape {
+    uint32_t density_columns;  /* mu_s columns per scattering-density tile */
+    uint32_t density_rows;     /* mu rows per scattering-density tile */
+    uint32_t density_variant;  /* occupancy variant of the density kernel (0, 1) */
+    uint32_t multiple_variant; /* occupancy variant of the multiple-scattering kernel */
+    float density_ms;          /* measured time of the chosen density launch */
+    float multiple_ms;         /* measured time of the chosen multiple-scattering launch */
+} fb_tile_shape;
+
+/* Times every candidate tile shape and kernel variant of each class in
+ * `classes` (its scattering sizes and precision count; `batch` atmospheres per
+ * measurement) on the builder's device and keeps the fastest for builds of
+ * that class. */
+int fb_builder_autotune(fb_builder* b, const fb_params* classes, uint32_t count,
+                        uint32_t batch);
+/* The shape builds of this class use; FB_ERR_NOT_FOUND if never tuned. */
+int fb_builder_tuned_shape(const fb_builder* b, const fb_params* cls,
+                           fb_tile_shape* out);
+/* JSON cache of the tuned shapes (one object per class). */
+int fb_builder_save_tuning(fb_builder* b, const char* path);
+int fb_builder_load_tuning(fb_builder* b, const char* path);
+
 /* ---- serving ------------------------------------------------------------- */
 
 /* A request loop over one builder: precompute requests arrive at any time and

@@ -71,7 +71,7 @@ def test_identical_requests_share_one_build(builder):
 def test_request_over_budget_is_rejected(builder):
     from fuzzyblue_gb300 import _native as N
     from fuzzyblue_gb300.api import Server
-    with Server(builder, hbm_budget_bytes=1 << 20) as srv:
+    with Server(builder, hbm_budget_bytes=64 << 10) as srv:
         with pytest.raises(N.FuzzyblueError) as ei:
             srv.submit(smoke_parameters())
         assert ei.value.status == N.FB_ERR_BUDGET
