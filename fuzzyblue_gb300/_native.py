@@ -143,6 +143,7 @@ SIGNATURES = {
     "fb_atmosphere_params": (_I, [_V, _P]),
     "fb_atmosphere_destroy": (None, [_V]),
     "fb_batch_build": (_I, [_V, _V, _P, _U32, ctypes.POINTER(_V)]),
+    "fb_atmosphere_build_noalloc": (_I, [_V, _P, _V, _V, _V]),
     "fb_builder_set_profiling": (_I, [_V, _I]),
     "fb_builder_autotune": (_I, [_V, _P, _U32, _U32]),
     "fb_builder_tuned_shape": (_I, [_V, _P, ctypes.POINTER(c_tile_shape)]),

@@ -7,6 +7,7 @@ Translation units are compiled in parallel with nvcc, one -gencode each:
   csrc/fb_util.cu           f16 export, tile-shape defaults
   csrc/fb_serve.cu          request loop with HBM admission and a resident LUT cache
   csrc/fb_tune.cu           tile-shape autotuner
+  csrc/fb_noalloc.cu        a build that allocates nothing (fixed device scratch)
 """
 import concurrent.futures as cf
 import os
@@ -31,6 +32,7 @@ UNITS = {
     "fb_util.cu": [],
     "fb_serve.cu": [],
     "fb_tune.cu": [],
+    "fb_noalloc.cu": [],
 }
 
 

@@ -793,6 +793,11 @@ int build(fb_builder* b, cudaStream_t s, const fb_params* params, uint32_t count
   return FB_OK;
 }
 
+void fill_atmo_record(fb::DevAtmo& d, const fb_params& p) {
+  Tuning untuned;
+  fill_devatmo(d, p, untuned);
+}
+
 fb_atmosphere* pending_detach(fb_pending* p, uint32_t i) {
   if (!p || i >= p->atms.size()) return nullptr;
   fb_atmosphere* a = p->atms[i];

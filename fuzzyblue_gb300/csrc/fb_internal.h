@@ -59,3 +59,14 @@ size_t atmosphere_bytes(const fb_atmosphere* a);
 cudaError_t launch_to_half(const float4* src, void* dst, size_t n, cudaStream_t s);
 
 }  // namespace fbi
+
+namespace fb {
+struct DevAtmo;
+}
+
+namespace fbi {
+// The kernels' record of one atmosphere with the default tile shapes (no
+// tables set).
+void fill_atmo_record(fb::DevAtmo& d, const fb_params& p);
+
+}  // namespace fbi

@@ -1,0 +1,216 @@
+// fb_noalloc.cu — fb_atmosphere_build_noalloc: one atmosphere built without
+// any device allocation.
+//
+// Who needs this: callers that may not allocate device memory, neither
+// directly nor through a library. Examples are an engine that owns every
+// device allocation through its own pool and forbids outside allocations, and
+// a render loop in which the device-wide synchronisation that an allocation
+// can imply would stall frames. They hand in the three output tables they own;
+// every temporary of the build (work lists, the order-to-order tables, the
+// FP64 accumulators of the mixed mode) lives in one fixed scratch array,
+// g_scratch below, that every GPU which loads this library holds until the
+// process exits.
+//
+// Limits and rules: the scratch holds kNoAllocScratchBytes (16 MiB), enough
+// for the r16 mu64 mu_s16 nu4 class in either precision; larger builds are
+// refused with FB_ERR_BUDGET. All calls share the array and it keeps the last
+// call's contents, so each call clears what must start at zero (the work
+// counters; every table is written before it is read), and calls whose GPU
+// work overlaps race on it: serialise them (one stream, or events). The first
+// call on a device sets that device up (looks up the scratch address and
+// raises the kernels' shared-memory limits); make that first call before any
+// stream capture.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "../../include/fuzzyblue.h"
+#include "fb_internal.h"
+#include "fb_kernels.h"
+
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = 16u << 20;
+constexpr int kMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_scratch[kNoAllocScratchBytes];
+
+struct DeviceSetup {
+  bool done = false;
+  unsigned char* scratch = nullptr;  // device address of g_scratch
+  int sms = 0;
+  int smem_optin = 0;
+};
+
+std::mutex g_setup_mu;
+DeviceSetup g_setup[kMaxDevices];
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Once per device, with that device current.
+int setup_device(int dev, DeviceSetup** out) {
+  std::lock_guard<std::mutex> g(g_setup_mu);
+  DeviceSetup& d = g_setup[dev];
+  if (!d.done) {
+    void* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_scratch);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return fbi::set_error(FB_ERR_CUDA, "cudaGetSymbolAddress of the no-alloc scratch failed");
+    }
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, dev) != cudaSuccess) {
+      cudaGetLastError();
+      return fbi::set_error(FB_ERR_CUDA, "cudaGetDeviceProperties failed");
+    }
+    for (int mode = 0; mode < 2; ++mode)
+      for (int pass = 0; pass < 4; ++pass)
+        for (int tpt : {1, 2, 4, 8}) {
+          const void* k = fb::kernel_for(mode == 1, pass, tpt, 0);
+          cudaFuncAttributes fa;
+          if (cudaFuncGetAttributes(&fa, k) != cudaSuccess ||
+              cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)prop.sharedMemPerBlockOptin - (int)fa.sharedSizeBytes) != cudaSuccess) {
+            cudaGetLastError();
+            return fbi::set_error(FB_ERR_NO_KERNEL, "no sm_103a kernel image loads on this device");
+          }
+        }
+    d.scratch = static_cast<unsigned char*>(ptr);
+    d.sms = prop.multiProcessorCount;
+    d.smem_optin = (int)prop.sharedMemPerBlockOptin;
+    d.done = true;
+  }
+  *out = &d;
+  return FB_OK;
+}
+
+struct Launch {
+  const void* fn;
+  fb::LaunchArgs args;
+  int block;
+  size_t smem;
+  int total;
+};
+
+}  // namespace
+
+extern "C" int fb_atmosphere_build_noalloc(void* stream, const fb_params* p, void* transmittance, void* irradiance,
+                                           void* scattering) {
+  if (!p || !transmittance || !irradiance || !scattering)
+    return fbi::set_error(FB_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (((uintptr_t)transmittance | (uintptr_t)irradiance | (uintptr_t)scattering) & 15u)
+    return fbi::set_error(FB_ERR_INVALID_ARGUMENT, "output tables must be 16-byte aligned");
+  int rc = fb_params_validate(p);
+  if (rc) return rc;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    cudaGetLastError();
+    return fbi::set_error(FB_ERR_CUDA, "no current CUDA device");
+  }
+  DeviceSetup* ds = nullptr;
+  rc = setup_device(dev, &ds);
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+
+  // layout of the scratch: record, work lists, counters, temporaries
+  const fbi::TableSizes z = fbi::sizes_of(*p);
+  const bool mixed = p->precision == FB_PRECISION_MIXED;
+  const int max_launches = 2 + 2 * 64;
+  const int n_ints = 2 * 2 * max_launches;  // per launch and segment: one job id, one offset
+  size_t off = 0;
+  const size_t o_atm = off;
+  off = align256(off + sizeof(fb::DevAtmo));
+  const size_t o_ints = off;
+  off = align256(off + sizeof(int) * n_ints);
+  const size_t o_cnt = off;
+  off = align256(off + sizeof(unsigned) * max_launches);
+  const size_t o_tmp = off;
+  off += z.tmp_bytes;
+  if (off > kNoAllocScratchBytes) {
+    char msg[160];
+    snprintf(msg, sizeof(msg), "this build needs %zu bytes of scratch; the fixed no-alloc scratch holds %zu", off,
+             kNoAllocScratchBytes);
+    return fbi::set_error(FB_ERR_BUDGET, msg);
+  }
+  unsigned char* base = ds->scratch;
+  fb::DevAtmo d;
+  fbi::fill_atmo_record(d, *p);
+  d.tr = (float4*)transmittance;
+  d.ir = (float4*)irradiance;
+  d.sc = (float4*)scattering;
+  unsigned char* tp = base + o_tmp;
+  d.dirr[0] = (float4*)tp; tp += align256(16 * z.nir);
+  d.dirr[1] = (float4*)tp; tp += align256(16 * z.nir);
+  d.dr = (float4*)tp;      tp += align256(16 * z.nsc);
+  d.dm = (float4*)tp;      tp += align256(16 * z.nsc);
+  d.dms = (float4*)tp;     tp += align256(16 * z.nsc);
+  d.dens = (float4*)tp;    tp += align256(16 * z.nsc);
+  if (mixed) {
+    d.sc_acc = (double*)tp; tp += align256(24 * z.nsc);
+    d.ir_acc = (double*)tp;
+  }
+  // launches of the pass order (src/precompute.rs:1726-1999), one job each
+  std::vector<int> ints(n_ints, 0);  // job ids 0, offsets 0
+  const fb::DevAtmo* d_atm = (const fb::DevAtmo*)(base + o_atm);
+  const int* d_ints = (const int*)(base + o_ints);
+  unsigned* d_cnt = (unsigned*)(base + o_cnt);
+  std::vector<Launch> L;
+  auto add = [&](int pass, int order, int nseg, int t0, int t1, size_t smem, int tpt) {
+    Launch l;
+    std::memset(&l, 0, sizeof(l));
+    l.fn = fb::kernel_for(mixed, pass, tpt, 0);
+    l.block = pass == fb::kPassDensity ? fb::kDensThreads : fb::kThreads;
+    l.smem = smem;
+    l.args.atm = d_atm;
+    l.args.nseg = nseg;
+    l.args.order = order;
+    l.args.counter = d_cnt + L.size();
+    const int tiles[2] = {t0, t1};
+    for (int sgi = 0; sgi < nseg; ++sgi) {
+      l.args.seg[sgi].njobs = 1;
+      l.args.seg[sgi].total = tiles[sgi];
+      l.args.seg[sgi].job = d_ints + 4 * L.size() + 2 * sgi;
+      l.args.seg[sgi].off = d_ints + 4 * L.size() + 2 * sgi + 1;
+    }
+    l.total = t0 + (nseg > 1 ? t1 : 0);
+    L.push_back(l);
+  };
+  add(fb::kPassTransmittance, 0, 1, fb::tiles_transmittance(d.tr_mu, d.tr_r), 0, 0, 1);
+  add(fb::kPassSingle, 0, 2, fb::tiles_rows(d.W, d.sc_mu, d.sc_r), fb::tiles_direct(d.ir_mus, d.ir_r),
+      fb::ss_smem(d.W, d.ss_steps, d.sc_mus, d.sc_nu), 1);
+  for (int n = 2; n <= d.order; ++n) {
+    const size_t sm = std::max(fb::density_smem(d, n == 2, mixed), fb::indirect_smem(d.irr_n, d.sc_nu, n - 1 == 1));
+    add(fb::kPassDensity, n, 2, fb::tiles_density(d), fb::tiles_indirect(d.ir_mus, d.ir_r), sm, 1);
+    add(fb::kPassMultiple, n, 1, fb::tiles_rows(d.W, d.sc_mu, d.sc_r), 0,
+        fb::ms_smem(d.W, d.ms_steps, d.sc_mus, d.sc_nu), fb::tpt_for_width(d.W));
+  }
+  cudaError_t e = cudaMemcpyAsync(base + o_atm, &d, sizeof(d), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(base + o_ints, ints.data(), sizeof(int) * n_ints, cudaMemcpyHostToDevice, st);
+  // the work counters are the only scratch that must start at zero
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_cnt, 0, sizeof(unsigned) * L.size(), st);
+  for (size_t k = 0; e == cudaSuccess && k < L.size(); ++k) {
+    cudaFuncAttributes fa;
+    e = cudaFuncGetAttributes(&fa, L[k].fn);
+    if (e != cudaSuccess) break;
+    if ((int)(L[k].smem + fa.sharedSizeBytes) > ds->smem_optin) {
+      return fbi::set_error(FB_ERR_INVALID_PARAMS, "shared memory of a pass exceeds the device limit");
+    }
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, L[k].fn, L[k].block, L[k].smem);
+    if (e != cudaSuccess) break;
+    const int grid = std::max(1, std::min(L[k].total, std::max(per_sm, 1) * ds->sms));
+    void* args[] = {(void*)&L[k].args};
+    e = cudaLaunchKernel(L[k].fn, dim3(grid), dim3(L[k].block), args, L[k].smem, st);
+  }
+  if (e != cudaSuccess) {
+    const char* m = cudaGetErrorString(e);
+    cudaGetLastError();
+    return fbi::set_error(FB_ERR_CUDA, m);
+  }
+  return FB_OK;
+}

@@ -250,6 +250,23 @@ int fb_atmosphere_params(const fb_atmosphere* a, fb_params* out);
 /* Drop for Atmosphere (src/precompute.rs:1059-1075). */
 void fb_atmosphere_destroy(fb_atmosphere* a);
 
+/* Builds one atmosphere without allocating any device memory. No counterpart
+ * in the reference: it exists for callers that may not allocate, directly or
+ * through a library, such as an engine that owns every device allocation in
+ * its own pool, or a render loop where an allocation's implicit device
+ * synchronisation would stall frames. The caller passes the three output
+ * tables (device pointers, 16-byte aligned, laid out as fb_tables describes);
+ * every temporary lives in a fixed 16 MiB device array that each GPU loading
+ * this library holds until the process exits. Builds needing more (beyond the
+ * r16 mu64 mu_s16 nu4 class) are refused with FB_ERR_BUDGET. The work is
+ * enqueued on `stream` for the current device. All calls share that array
+ * and it keeps the last call's contents: calls whose GPU work overlaps race on
+ * it, so serialise them. The first call on a device sets the device up; make
+ * it before any stream capture. */
+int fb_atmosphere_build_noalloc(void* stream, const fb_params* p,
+                                void* transmittance, void* irradiance,
+                                void* scattering);
+
 /* ---- batches ------------------------------------------------------------- */
 
 /* Builds `count` atmospheres with one persistent launch per pass group,
