@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--batch", type=int, default=BATCH)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
     return ap.parse_args()
 
 
@@ -134,13 +135,24 @@ def max_over_ranks(world, v):
 
 
 # ------------------------------------------------------------- roofline ---
-# Work of the dominant kernel (scattering density + indirect irradiance): the
-# unit is one direction evaluation of the scattering-density integrand
-# (scattering_density.comp:62-104), 2 * density_samples^2 directions per texel,
-# plus 16 x 64 per irradiance texel. FLOPs per direction evaluation of the
-# kernel's algorithm (order >= 3, counted in fb_passes.cuh tile_density's inner
-# loop: FP32 adds, multiplies and FMAs as 2, MUFU ops as 1).
-FLOP_PER_DIRECTION = 46.0
+# Algorithmic FLOPs: the shader arithmetic of the reference's algorithm per
+# output texel, op-counted on the oracle's restatement over the first 16
+# atmospheres of this workload (`python oracle/count_flops.py`; adds, muls,
+# divs, sqrts and transcendentals one FLOP each, sampler filtering and
+# literal-only expressions not counted). The dominant launch computes the
+# scattering density of order n (2 * 16^2 directions per texel, 162.6 FLOPs
+# per direction at n >= 3) and the indirect irradiance of order n - 1.
+FLOP_PER_TEXEL = {
+    "transmittance": 28311.7,
+    "direct_irradiance": 34.0,
+    "single_scattering": 8033.8,
+    "density_order2": 133663.8,
+    "density_order3": 83260.2,
+    "indirect_order1": 163843.0,
+    "indirect_order2": 74755.0,
+    "multiple_scattering": 8332.2,
+}
+FLOP_PER_ATMOSPHERE = 350185724984.0  # default sizes, 4 orders (same count)
 
 
 def fp32_peak_tflops(sms, mhz):
@@ -186,6 +198,12 @@ def run_ours(a):
         builder.set_profiling(profile)
         pend = build_batch(builder, params, stream=stream)
         return pend
+
+    # tile shapes of the workload's table class from the autotuner (untimed)
+    tuned = None
+    if not a.no_autotune:
+        builder.autotune([params[0]], batch=8)
+        tuned = builder.tuned_shape(params[0])
 
     # warm-up (graph path)
     for _ in range(a.warmup):
@@ -284,9 +302,8 @@ def run_ours(a):
     dens = [r for launches in prof for r in launches if r["kernel"] == "density+indirect" and r["order"] >= 3]
     dens_ms = sum(r["ms"] for r in dens) / max(len(dens), 1)
     sms = builder.sm_count
-    dirs = 2 * params[0].density_samples ** 2
-    units = a.batch * (sizes[2] * dirs + sizes[1] * 16 * 64)
-    achieved = units * FLOP_PER_DIRECTION / (dens_ms / 1e3) / 1e12
+    flops = a.batch * (sizes[2] * FLOP_PER_TEXEL["density_order3"] + sizes[1] * FLOP_PER_TEXEL["indirect_order2"])
+    achieved = flops / (dens_ms / 1e3) / 1e12
     mhz = (clk or {}).get("sm_mhz") or 2070.0
     peak = fp32_peak_tflops(sms, mhz)
     traffic = read_traffic()
@@ -317,7 +334,9 @@ def run_ours(a):
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                      "peak_source": "152 SMs x 128 FP32 lanes x 2 FLOP x median SM clock under load (%d MHz); "
                                     "the kernel uses neither HBM bandwidth nor tensor cores at their limits" % mhz,
-                     "launch_ms": dens_ms, "flop_per_direction": FLOP_PER_DIRECTION,
+                     "launch_ms": dens_ms, "flop_per_launch": flops,
+                     "flop_source": "reference shader arithmetic per texel, op-counted on the oracle "
+                                    "(oracle/count_flops.py)",
                      "hbm": {"achieved_gbs": (traffic or 0) / (dens_ms / 1e3) / 1e9 if traffic else None,
                              "peak_gbs": peaks.get("hbm_gbs"), "peak_source": "MEASURED_PEAKS.json"},
                      "traffic": traffic},
@@ -326,6 +345,8 @@ def run_ours(a):
         "graph": {"ms_per_step": graph_ms, "value": world * a.batch / (graph_ms / 1e3)},
         "plain": {"ms_per_atmosphere": plain_ms, "atmospheres_per_s": 1e3 / plain_ms, "precision": "plain"},
         "batched_over_plain": value / (world * 1e3 / plain_ms),
+        "algorithmic_tflops": value * FLOP_PER_ATMOSPHERE / 1e12,
+        "tile_shape": tuned,
     }
     if rank == 0 and not a.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(params[0])

@@ -16,6 +16,7 @@
 
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 namespace {
@@ -37,6 +38,85 @@ template <> struct Num<double> {
   static double cos(double x) { return std::cos(x); }
   static double sin(double x) { return std::sin(x); }
   static double floor(double x) { return std::floor(x); }
+};
+
+// --------------------------------------------------------- op counting ---
+// CF: an FP32 scalar that tallies the arithmetic done on it, used only by
+// fbo_count_ops to measure the FLOPs per texel of each pass of the reference's
+// algorithm. Operations whose operands are all compile-time literals are folded
+// (not counted), as a shader compiler folds them; operations that involve a
+// uniform (atmosphere parameter), a texel coordinate or a table value count.
+struct OpTally {
+  uint64_t add = 0, mul = 0, div = 0, sqrt = 0, transc = 0;
+  bool on = true;
+};
+thread_local OpTally g_tally;
+
+struct CF {
+  float v = 0.f;
+  bool lit = true;  // value of literals only
+  CF() = default;
+  CF(double x) : v((float)x) {}
+  CF(float x) : v(x) {}
+  CF(int x) : v((float)x) {}
+  CF(unsigned x) : v((float)x) {}
+  static CF var(float x) {
+    CF c(x);
+    c.lit = false;
+    return c;
+  }
+  explicit operator float() const { return v; }
+  explicit operator double() const { return v; }
+  explicit operator int() const { return (int)v; }
+};
+inline CF tallied(uint64_t& n, float v, const CF& a, const CF& b) {
+  CF o(v);
+  o.lit = a.lit && b.lit;
+  if (!o.lit && g_tally.on) ++n;
+  return o;
+}
+inline CF operator+(CF a, CF b) { return tallied(g_tally.add, a.v + b.v, a, b); }
+inline CF operator-(CF a, CF b) { return tallied(g_tally.add, a.v - b.v, a, b); }
+inline CF operator*(CF a, CF b) { return tallied(g_tally.mul, a.v * b.v, a, b); }
+inline CF operator/(CF a, CF b) { return tallied(g_tally.div, a.v / b.v, a, b); }
+inline CF operator-(CF a) {
+  CF o(-a.v);
+  o.lit = a.lit;
+  return o;
+}
+inline bool operator<(CF a, CF b) { return a.v < b.v; }
+inline bool operator>(CF a, CF b) { return a.v > b.v; }
+inline bool operator<=(CF a, CF b) { return a.v <= b.v; }
+inline bool operator>=(CF a, CF b) { return a.v >= b.v; }
+inline bool operator==(CF a, CF b) { return a.v == b.v; }
+inline CF tallied1(uint64_t& n, float v, const CF& a) {
+  CF o(v);
+  o.lit = a.lit;
+  if (!o.lit && g_tally.on) ++n;
+  return o;
+}
+template <> struct Num<CF> {
+  static CF sqrt(CF x) { return tallied1(g_tally.sqrt, std::sqrt(x.v), x); }
+  static CF exp(CF x) { return tallied1(g_tally.transc, std::exp(x.v), x); }
+  static CF pow(CF x, CF y) { return tallied(g_tally.transc, std::pow(x.v, y.v), x, y); }
+  static CF cos(CF x) { return tallied1(g_tally.transc, std::cos(x.v), x); }
+  static CF sin(CF x) { return tallied1(g_tally.transc, std::sin(x.v), x); }
+  static CF floor(CF x) {
+    CF o(std::floor(x.v));
+    o.lit = x.lit;
+    return o;
+  }
+};
+// A value that is uniform over a dispatch (an atmosphere parameter).
+template <class T> inline T uni(float x) { return T(x); }
+template <> inline CF uni<CF>(float x) { return CF::var(x); }
+// Texture filtering is fixed-function sampler work in the reference, not
+// shader arithmetic: it is not counted.
+template <class T> struct SamplerWork {};
+template <> struct SamplerWork<CF> {
+  bool saved;
+  SamplerWork() : saved(g_tally.on) { g_tally.on = false; }
+  ~SamplerWork() { g_tally.on = saved; }
 };
 
 // GLSL min/max/clamp as specified (min: y < x ? y : x; max: x < y ? y : x).
@@ -73,17 +153,17 @@ template <class T> struct Atmo {
   bool exact_altitude;  // FP64 oracle: clamp rounding-negative altitudes (see optical_length)
 };
 
-template <class T> V3<T> v3(const float* f) { return V3<T>(T(f[0]), T(f[1]), T(f[2])); }
+template <class T> V3<T> v3(const float* f) { return V3<T>(uni<T>(f[0]), uni<T>(f[1]), uni<T>(f[2])); }
 template <class T> Profile<T> prof(const fb_density_profile& p) {
   Profile<T> o;
   const fb_density_profile_layer* L[2] = {&p.layers[0], &p.layers[1]};
   Layer<T>* D[2] = {&o.lo, &o.hi};
   for (int i = 0; i < 2; ++i) {
-    D[i]->width = T(L[i]->width);
-    D[i]->exp_term = T(L[i]->exp_term);
-    D[i]->exp_scale = T(L[i]->exp_scale);
-    D[i]->linear_term = T(L[i]->linear_term);
-    D[i]->constant_term = T(L[i]->constant_term);
+    D[i]->width = uni<T>(L[i]->width);
+    D[i]->exp_term = uni<T>(L[i]->exp_term);
+    D[i]->exp_scale = uni<T>(L[i]->exp_scale);
+    D[i]->linear_term = uni<T>(L[i]->linear_term);
+    D[i]->constant_term = uni<T>(L[i]->constant_term);
   }
   return o;
 }
@@ -97,11 +177,11 @@ template <class T> Atmo<T> load(const fb_params* p) {
   a.mie_ext = v3<T>(r.mie_extinction);
   a.albedo = v3<T>(r.ground_albedo);
   a.absorption = v3<T>(r.absorption_extinction);
-  a.sun_radius = T(r.sun_angular_radius);
-  a.bottom = T(r.bottom_radius);
-  a.top = T(r.top_radius);
-  a.g = T(r.mie_phase_function_g);
-  a.mu_s_min = T(r.mu_s_min);
+  a.sun_radius = uni<T>(r.sun_angular_radius);
+  a.bottom = uni<T>(r.bottom_radius);
+  a.top = uni<T>(r.top_radius);
+  a.g = uni<T>(r.mie_phase_function_g);
+  a.mu_s_min = uni<T>(r.mu_s_min);
   a.ray_d = prof<T>(r.rayleigh_density);
   a.mie_d = prof<T>(r.mie_density);
   a.abs_d = prof<T>(r.absorption_density);
@@ -120,7 +200,7 @@ template <class T> Atmo<T> load(const fb_params* p) {
   a.irr_n = (int)p->irradiance_samples;
   a.order = (int)p->order;
   a.f16 = p->storage == FB_STORAGE_F16;
-  a.exact_altitude = sizeof(T) == sizeof(double);
+  a.exact_altitude = std::is_same<T, double>::value;
   return a;
 }
 
@@ -213,6 +293,7 @@ template <class T> inline void axis(T coord, int n, int& i0, int& i1, T& frac) {
 
 // Bilinear RGB fetch (src/precompute.rs:85-98 sampler; Vulkan weight order).
 template <class T> V3<T> fetch2(const Tab<T>& t, T u, T v) {
+  SamplerWork<T> not_shader_work;
   int x0, x1, y0, y1;
   T a, b;
   axis(u, t.w, x0, x1, a);
@@ -230,6 +311,7 @@ template <class T> V3<T> fetch2(const Tab<T>& t, T u, T v) {
 
 // Trilinear RGB fetch.
 template <class T> V3<T> fetch3(const Tab<T>& t, T u, T v, T s) {
+  SamplerWork<T> not_shader_work;
   int x0, x1, y0, y1, z0, z1;
   T a, b, c;
   axis(u, t.w, x0, x1, a);
@@ -751,6 +833,45 @@ int indirect_impl(const fb_params* p, int nthreads, int order, const T* sr, cons
 
 }  // namespace
 
+// Op counts of the reference's algorithm: runs one pass's texel routine over
+// `n` texels drawn uniformly (fixed LCG from `seed`) with CF scalars on zero
+// tables (the arithmetic does not depend on table values), and returns the
+// mean per texel of: adds/subs, muls, divs, sqrts, transcendentals (exp, pow,
+// cos, sin). Sampler filtering is excluded (see SamplerWork).
+int count_ops(const fb_params* p, int pass, int order, int64_t n, uint64_t seed, double* out) {
+  if (!valid(p) || !out || n <= 0 || pass < 0 || pass > 5) return FB_ERR_INVALID_ARGUMENT;
+  const Atmo<CF> a = load<CF>(p);
+  const int64_t ntr = (int64_t)a.tr_mu * a.tr_r, nir = (int64_t)a.ir_mus * a.ir_r;
+  const int64_t nsc = (int64_t)a.sc_nu * a.sc_mus * a.sc_mu * a.sc_r;
+  const int W = a.sc_nu * a.sc_mus;
+  std::vector<CF> tr(4 * ntr, CF::var(0.f)), ir(4 * nir, CF::var(0.f)), sc(4 * nsc, CF::var(0.f));
+  const Tab<CF> ttr = tab<CF>(tr.data(), a.tr_mu, a.tr_r), tir = tab<CF>(ir.data(), a.ir_mus, a.ir_r);
+  const Tab<CF> tsc = tab<CF>(sc.data(), W, a.sc_mu, a.sc_r);
+  const int64_t count[6] = {ntr, nir, nsc, nsc, nir, nsc};
+  g_tally = OpTally();
+  uint64_t st = seed * 6364136223846793005ull + 1442695040888963407ull;
+  CF o[4], o2[4], ph;
+  for (int64_t k = 0; k < n; ++k) {
+    st = st * 6364136223846793005ull + 1442695040888963407ull;
+    const int64_t t = (int64_t)((st >> 17) % (uint64_t)count[pass]);
+    switch (pass) {
+      case 0: transmittance_texel(a, t, o); break;
+      case 1: direct_irradiance_texel(a, ttr, t, o); break;
+      case 2: single_scattering_texel(a, ttr, t, o, o2); break;
+      case 3: density_texel(a, order, ttr, tsc, tsc, tsc, tir, t, o); break;
+      case 4: indirect_texel(a, order, tsc, tsc, tsc, t, o); break;
+      default: multiple_texel(a, ttr, tsc, t, o, &ph); break;
+    }
+  }
+  const double dn = (double)n;
+  out[0] = g_tally.add / dn;
+  out[1] = g_tally.mul / dn;
+  out[2] = g_tally.div / dn;
+  out[3] = g_tally.sqrt / dn;
+  out[4] = g_tally.transc / dn;
+  return FB_OK;
+}
+
 extern "C" {
 
 int fbo_precompute_f32(const fb_params* p, int nthreads, float* tr, float* ir, float* sc, float* oms,
@@ -860,6 +981,14 @@ void fbo_params_default(fb_params* o) {
   o->irradiance_samples = 32;
   o->precision = FB_PRECISION_PLAIN;
   o->storage = FB_STORAGE_F32;
+}
+
+// Shader arithmetic per texel of pass `pass` (0 transmittance, 1 direct
+// irradiance, 2 single scattering, 3 scattering density of `order`, 4 indirect
+// irradiance of `order`, 5 multiple scattering): out[5] = adds, muls, divs,
+// sqrts, transcendentals, averaged over n sampled texels.
+int fbo_count_ops(const fb_params* p, int pass, int order, int64_t n, uint64_t seed, double* out) {
+  return count_ops(p, pass, order, n, seed, out);
 }
 
 }  // extern "C"

@@ -105,6 +105,15 @@ int fbo_multiple_scattering_f64(const fb_params* p, int nthreads,
  * default sample counts, for callers that do not link the library. */
 void fbo_params_default(fb_params* out);
 
+/* Reference shader arithmetic per texel of one pass (0 transmittance, 1 direct
+ * irradiance, 2 single scattering, 3 scattering density of `order`, 4 indirect
+ * irradiance of `order`, 5 multiple scattering), averaged over `n` sampled
+ * texels: out[5] = adds/subs, muls, divs, sqrts, transcendentals. Sampler
+ * filtering (fixed-function in the reference) is not counted; operations on
+ * literals only are folded. */
+int fbo_count_ops(const fb_params* p, int pass, int order, int64_t n,
+                  uint64_t seed, double* out);
+
 #ifdef __cplusplus
 }
 #endif

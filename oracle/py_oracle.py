@@ -50,6 +50,7 @@ def lib():
         L.fbo_multiple_scattering_f32.argtypes = [P, ctypes.c_int, _F, _F, _I, ctypes.c_int64, _F, _F]
         L.fbo_multiple_scattering_f64.argtypes = [P, ctypes.c_int, _D, _D, _I, ctypes.c_int64, _D, _D]
         L.fbo_params_default.argtypes = [P]
+        L.fbo_count_ops.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int64, ctypes.c_uint64, _D]
         _lib = L
     return _lib
 
@@ -212,3 +213,21 @@ def default_params_c() -> c_params:
     c = c_params()
     lib().fbo_params_default(ctypes.byref(c))
     return c
+
+
+PASSES = ("transmittance", "direct_irradiance", "single_scattering", "scattering_density",
+          "indirect_irradiance", "multiple_scattering")
+
+
+def count_ops(p: Parameters, pass_name: str, order: int = 3, samples: int = 256, seed: int = 0) -> dict:
+    """Shader arithmetic per texel of one pass of the reference's algorithm
+    (oracle op count; sampler filtering excluded): adds, muls, divs, sqrts,
+    transcendentals, and `flops`, their sum."""
+    out = np.zeros(5, np.float64)
+    c = p.to_c()
+    _check(lib().fbo_count_ops(ctypes.byref(c), PASSES.index(pass_name), order, samples, seed, _ptr(out, _D)),
+           "fbo_count_ops")
+    d = dict(zip(("add", "mul", "div", "sqrt", "transc"), out.tolist()))
+    d["flops"] = float(out.sum())
+    return d
+

@@ -147,3 +147,19 @@ def test_oracle_rejects_invalid(oracle):
     p = smoke_parameters().replace(scattering_mu_size=31)
     with pytest.raises(RuntimeError):
         oracle.precompute(p)
+
+
+def test_op_count_of_branch_free_passes_is_exact(oracle):
+    """The op-counting instantiation of the oracle (the algorithmic FLOPs of
+    the roofline): indirect irradiance has no data-dependent branch, so every
+    texel costs the same; density of order 2 (two tables, two phase functions
+    per lookup) costs more than order 3; counts do not depend on the seed."""
+    p = Parameters()
+    a = oracle.count_ops(p, "indirect_irradiance", 2, 64, 1)
+    b = oracle.count_ops(p, "indirect_irradiance", 2, 64, 7)
+    assert a == b and a["flops"] == int(a["flops"]) and a["flops"] > 0
+    d2 = oracle.count_ops(p, "scattering_density", 2, 8, 3)
+    d3 = oracle.count_ops(p, "scattering_density", 3, 8, 3)
+    assert d2["flops"] > d3["flops"] > 512 * 50
+    # 16 x 64 hemisphere directions, one transcendental-free table lookup each
+    assert a["transc"] == 0 and a["sqrt"] == 4 * 1024
