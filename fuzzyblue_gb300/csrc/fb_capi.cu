@@ -146,6 +146,27 @@ extern "C" int fb_params_extents(const fb_params* p, fb_extent* tr, fb_extent* i
 
 namespace fbi {
 
+// Geometry tables (order-independent, written by the first two launches):
+// rows, x columns, multiple-scattering sample records, density r / theta records.
+size_t geometry_bytes(const fb_params& p) {
+  const fb_params_raw& r = p.raw;
+  const size_t rows = (size_t)r.scattering_mu_size * r.scattering_r_size;
+  const size_t W = (size_t)r.scattering_nu_size * r.scattering_mu_s_size;
+  return align256(sizeof(fb::RowGeo) * rows) + align256(sizeof(fb::ColGeo) * W) +
+         align256(sizeof(fb::MSRec) * rows * (p.multiple_scattering_steps + 1)) +
+         align256(sizeof(fb::DensZ) * r.scattering_r_size) +
+         align256(sizeof(fb::ThetaRec) * r.scattering_r_size * p.density_samples);
+}
+
+void place_geometry(fb::DevAtmo& d, char*& tp) {
+  const size_t rows = (size_t)d.sc_mu * d.sc_r;
+  d.g_rows = (fb::RowGeo*)tp;   tp += align256(sizeof(fb::RowGeo) * rows);
+  d.g_cols = (fb::ColGeo*)tp;   tp += align256(sizeof(fb::ColGeo) * (size_t)d.W);
+  d.g_ms = (fb::MSRec*)tp;      tp += align256(sizeof(fb::MSRec) * rows * (d.ms_steps + 1));
+  d.g_z = (fb::DensZ*)tp;       tp += align256(sizeof(fb::DensZ) * (size_t)d.sc_r);
+  d.g_th = (fb::ThetaRec*)tp;   tp += align256(sizeof(fb::ThetaRec) * (size_t)d.sc_r * d.dens_n);
+}
+
 TableSizes sizes_of(const fb_params& p) {
   const fb_params_raw& r = p.raw;
   TableSizes s;
@@ -155,6 +176,7 @@ TableSizes sizes_of(const fb_params& p) {
   s.out_bytes = align256(16 * s.ntr) + align256(16 * s.nir) + align256(16 * s.nsc);
   s.tmp_bytes = 2 * align256(16 * s.nir) + 4 * align256(16 * s.nsc);
   if (p.precision == FB_PRECISION_MIXED) s.tmp_bytes += align256(24 * s.nsc) + align256(24 * s.nir);
+  s.tmp_bytes += geometry_bytes(p);
   return s;
 }
 
@@ -436,10 +458,10 @@ struct PlannedLaunch {
   int variant;
   int order;
   int nseg;
-  int seg_njobs[2];
-  int seg_total[2];
-  size_t seg_job_off[2];  // offsets (in ints) into the int pool
-  size_t seg_off_off[2];
+  int seg_njobs[fb::kMaxSegments];
+  int seg_total[fb::kMaxSegments];
+  size_t seg_job_off[fb::kMaxSegments];  // offsets (in ints) into the int pool
+  size_t seg_off_off[fb::kMaxSegments];
   size_t smem;
   uint64_t texels;
 };
@@ -494,30 +516,39 @@ void plan_group(Plan& P, const std::vector<DevAtmo>& A, const std::vector<int>& 
     L.order = order;
     return L;
   };
-  {  // transmittance
+  {  // transmittance + geometry tables
     PlannedLaunch L = mk(fb::kPassTransmittance, 0);
-    std::vector<int> tiles;
+    std::vector<int> tiles, tg;
     for (int j : group) {
       tiles.push_back(fb::tiles_transmittance(A[j].tr_mu, A[j].tr_r));
+      tg.push_back(fb::tiles_geometry(A[j].W, A[j].sc_mu, A[j].sc_r));
       L.texels += (uint64_t)A[j].tr_mu * A[j].tr_r;
     }
     add_segment(P, L, 0, group, tiles);
-    L.nseg = 1;
+    add_segment(P, L, 1, group, tg);
+    L.nseg = 2;
     P.launches.push_back(L);
   }
-  {  // single scattering rows + direct irradiance
+  {  // single scattering rows + direct irradiance + records for the orders >= 2
     PlannedLaunch L = mk(fb::kPassSingle, 0);
-    std::vector<int> t0, t1;
+    std::vector<int> t0, t1, t2, t3, multi;
     for (int j : group) {
       const DevAtmo& a = A[j];
       t0.push_back(fb::tiles_rows(a.W, a.sc_mu, a.sc_r));
       t1.push_back(fb::tiles_direct(a.ir_mus, a.ir_r));
+      if (a.order >= 2) {
+        multi.push_back(j);
+        t2.push_back(fb::tiles_msrec(a.sc_mu, a.sc_r, a.ms_steps));
+        t3.push_back(fb::tiles_densgeo(a.sc_r, a.dens_n));
+      }
       L.smem = std::max(L.smem, fb::ss_smem(a.W, a.ss_steps, a.sc_mus, a.sc_nu));
       L.texels += (uint64_t)a.W * a.sc_mu * a.sc_r + (uint64_t)a.ir_mus * a.ir_r;
     }
     add_segment(P, L, 0, group, t0);
     add_segment(P, L, 1, group, t1);
-    L.nseg = 2;
+    add_segment(P, L, 2, multi, t2);
+    add_segment(P, L, 3, multi, t3);
+    L.nseg = 4;
     P.launches.push_back(L);
   }
   for (int n = 2; n <= max_order; ++n) {
@@ -675,6 +706,7 @@ int build(fb_builder* b, cudaStream_t s, const fb_params* params, uint32_t count
       d.sc_acc = (double*)tp; tp += align256(24 * z.nsc);
       d.ir_acc = (double*)tp; tp += align256(24 * z.nir);
     }
+    place_geometry(d, tp);
   }
   // work plan
   Plan plan;

@@ -23,6 +23,55 @@ struct Layer {
   float width, exp_term, exp_scale, linear_term, constant_term;
 };
 
+// One axis of the LINEAR + CLAMP_TO_EDGE sampler of src/precompute.rs:85-98:
+// the two neighbouring texels and the weight of the second.
+struct Axis {
+  int i0, i1;
+  float f;
+};
+
+// ---------------------------------------------------- geometry tables
+// Order-independent geometry of one atmosphere, computed once per build (the
+// FP64 decodes of the mixed mode cost 64 FP32 issue slots each on this part,
+// so no pass repeats them per tile or per order).
+
+// One (mu, r) row of the packed scattering table (texel y, z): the view ray.
+struct RowGeo {
+  float r, mu, dist, rr, two_r_mu, r_mu;  // PLAIN: the reference's float values; dist to the ground or the top
+  double q, s, distd, one_m_mu2, mud;     // MIXED: q = r^2 - R^2, s = r mu, FP64 distance, 1 - mu^2, mu
+  int ground, pad;
+};
+
+// One x column of the packed table (nu slice x / mu_s_size, mu_s index x % mu_s_size).
+struct ColGeo {
+  float mu_s, one_m_mus2, nu_raw, u_mus;  // PLAIN: reference float values; u_mus = u_mu_s texture coordinate
+  double mu_sd, one_m_mus2d, nu_rawd, t_musd;  // MIXED: FP64 values; t_musd = texel coordinate within a slice
+};
+
+// One trapezoid sample of multiple scattering along the view ray of a row.
+struct MSRec {
+  float d, inv_r, tvwx, tvwy, tvwz, fy, fz;  // distance, 1/r_i, transmittance x dx x weight, (mu, r) weights
+  int y0, y1, z0, z1, pad;
+};
+
+// Scattering density: per r slice, and per (r slice, theta row) of the sphere grid.
+struct DensZ {
+  float r;
+  int pad;
+  double q;
+  Axis az;   // r axis of the 3D tables
+  Axis irx;  // r axis of the irradiance table at the ground
+};
+struct DensTheta {
+  float cos_t, domega, dg, tgx, tgy, tgz;  // tg = transmittance to the ground x albedo / pi
+  int ground, pad;
+};
+struct ThetaRec {
+  DensTheta th;
+  Axis tay;  // mu axis of the lookup direction
+  int pad;
+};
+
 // One atmosphere as the kernels see it: parameters (ParamsRaw fields,
 // src/precompute.rs:937-964), sizes, sample counts and its tables.
 struct DevAtmo {
@@ -46,6 +95,12 @@ struct DevAtmo {
   float4* dens;     // scattering density of the current order
   double* sc_acc;   // MIXED: FP64 running sum of scattering rgb (3 per texel)
   double* ir_acc;   // MIXED: FP64 running sum of irradiance rgb (3 per texel)
+  // geometry tables (written by the transmittance and single-scattering launches)
+  RowGeo* g_rows;   // sc_mu * sc_r
+  ColGeo* g_cols;   // W
+  MSRec* g_ms;      // sc_mu * sc_r * (ms_steps + 1)
+  DensZ* g_z;       // sc_r
+  ThetaRec* g_th;   // sc_r * dens_n
 };
 
 constexpr float kPiF = 3.14159265358979323846f;
@@ -101,12 +156,7 @@ __device__ __forceinline__ float profile_density(const Layer* P, float h) {
 }
 
 // ------------------------------------------------------------ table access
-// One axis of the LINEAR + CLAMP_TO_EDGE sampler of src/precompute.rs:85-98:
-// texel coordinate u*n - 0.5, neighbours clamped to [0, n-1].
-struct Axis {
-  int i0, i1;
-  float f;
-};
+// make_axis: texel coordinate u*n - 0.5, neighbours clamped to [0, n-1].
 __device__ __forceinline__ Axis make_axis(float coord, int n) {
   float x = coord * float(n) - 0.5f;
   float fl = floorf(x);
@@ -527,17 +577,12 @@ struct TexelParams {
   bool ground;
 };
 
-// PLAIN: the reference's float arithmetic.
-__device__ __forceinline__ void decode_texel32(const DevAtmo& a, const Geo32& G, uint32_t ix, uint32_t iy,
-                                               uint32_t iz, float& r, float& mu, float& mu_s, float& nu,
-                                               bool& ground) {
-  const uint32_t W = (uint32_t)a.W;
-  float fx = frag_from_texel(ix, W), fy = frag_from_texel(iy, (uint32_t)a.sc_mu),
-        fz = frag_from_texel(iz, (uint32_t)a.sc_r);
-  float nmus = float(a.sc_mus);
-  float f_nu = floorf(fx / nmus);
-  float f_mus = fx - nmus * floorf(fx / nmus);
-  float qx = f_nu / float(a.sc_nu - 1), qy = f_mus / nmus, qz = fy / float(a.sc_mu), qw = fz / float(a.sc_r);
+// PLAIN: the reference's float arithmetic, split into the part that depends on
+// the row (y, z) and the part that depends on the column x.
+__device__ __forceinline__ void decode_yz32(const DevAtmo& a, const Geo32& G, uint32_t iy, uint32_t iz, float& r,
+                                            float& mu, bool& ground) {
+  float fy = frag_from_texel(iy, (uint32_t)a.sc_mu), fz = frag_from_texel(iz, (uint32_t)a.sc_r);
+  float qz = fy / float(a.sc_mu), qw = fz / float(a.sc_r);
   float rho = G.H * unit_from_coord(qw, a.sc_r);
   r = sqrtf(rho * rho + G.R * G.R);
   if (qz < 0.5f) {
@@ -553,6 +598,15 @@ __device__ __forceinline__ void decode_texel32(const DevAtmo& a, const Geo32& G,
     mu = d == 0.0f ? 1.0f : clamp_cosine((G.H * G.H - rho * rho - d * d) / (2.0f * r * d));
     ground = false;
   }
+}
+// mu_s and the nu of column x before the clamp of scattering.h:134-136.
+__device__ __forceinline__ void decode_x32(const DevAtmo& a, const Geo32& G, uint32_t ix, float& mu_s,
+                                           float& nu_raw) {
+  float fx = frag_from_texel(ix, (uint32_t)a.W);
+  float nmus = float(a.sc_mus);
+  float f_nu = floorf(fx / nmus);
+  float f_mus = fx - nmus * floorf(fx / nmus);
+  float qx = f_nu / float(a.sc_nu - 1), qy = f_mus / nmus;
   float x_mu_s = unit_from_coord(qy, a.sc_mus);
   float d_min = G.T - G.R;
   float d_max = G.H;
@@ -560,22 +614,27 @@ __device__ __forceinline__ void decode_texel32(const DevAtmo& a, const Geo32& G,
   float aa = (A - x_mu_s * A) / (1.0f + x_mu_s * A);
   float d = d_min + gmin(aa, A) * (d_max - d_min);
   mu_s = d == 0.0f ? 1.0f : clamp_cosine((G.H * G.H - d * d) / (2.0f * G.R * d));
-  nu = clamp_cosine(qx * 2.0f - 1.0f);
-  float sq = sqrtf((1.0f - mu * mu) * (1.0f - mu_s * mu_s));
-  nu = gclamp(nu, mu * mu_s - sq, mu * mu_s + sq);
+  nu_raw = clamp_cosine(qx * 2.0f - 1.0f);
+}
+// scattering.h:134-136: nu limited to the range that mu and mu_s allow.
+__device__ __forceinline__ float clamp_nu32(float nu_raw, float mu, float mu_s, float one_m_mus2) {
+  float sq = sqrtf((1.0f - mu * mu) * one_m_mus2);
+  return gclamp(nu_raw, mu * mu_s - sq, mu * mu_s + sq);
+}
+__device__ __forceinline__ void decode_texel32(const DevAtmo& a, const Geo32& G, uint32_t ix, uint32_t iy,
+                                               uint32_t iz, float& r, float& mu, float& mu_s, float& nu,
+                                               bool& ground) {
+  decode_yz32(a, G, iy, iz, r, mu, ground);
+  float nu_raw;
+  decode_x32(a, G, ix, mu_s, nu_raw);
+  nu = clamp_nu32(nu_raw, mu, mu_s, 1.0f - mu_s * mu_s);
 }
 
 // MIXED: the same decode in FP64, producing q and s directly.
-__device__ __forceinline__ TexelParams decode_texel64(const DevAtmo& a, const Geo64& G, uint32_t ix, uint32_t iy,
-                                                      uint32_t iz) {
-  TexelParams o;
-  const uint32_t W = (uint32_t)a.W;
-  double fx = frag_from_texel_d(ix, W), fy = frag_from_texel_d(iy, (uint32_t)a.sc_mu),
-         fz = frag_from_texel_d(iz, (uint32_t)a.sc_r);
-  double nmus = double(a.sc_mus);
-  double f_nu = floor(fx / nmus);
-  double f_mus = fx - nmus * floor(fx / nmus);
-  double qx = f_nu / double(a.sc_nu - 1), qy = f_mus / nmus, qz = fy / double(a.sc_mu), qw = fz / double(a.sc_r);
+__device__ __forceinline__ void decode_yz64(const DevAtmo& a, const Geo64& G, uint32_t iy, uint32_t iz,
+                                            TexelParams& o) {
+  double fy = frag_from_texel_d(iy, (uint32_t)a.sc_mu), fz = frag_from_texel_d(iz, (uint32_t)a.sc_r);
+  double qz = fy / double(a.sc_mu), qw = fz / double(a.sc_r);
   double rho = G.H * unit_from_coord(qw, a.sc_r);
   o.q = rho * rho;
   o.r = G.radius(o.q);
@@ -593,14 +652,28 @@ __device__ __forceinline__ TexelParams decode_texel64(const DevAtmo& a, const Ge
     o.ground = false;
   }
   o.mu = o.s / o.r;
-  double x_mu_s = unit_from_coord(qy, a.sc_mus);
-  double d_min = G.T - G.R;
-  double d_max = G.H;
+}
+// scattering.h:102-113 in FP64: mu_s and the raw nu of column x.
+__device__ __forceinline__ void decode_x64(const DevAtmo& a, const Geo64& G, uint32_t ix, double& mu_s,
+                                           double& nu_raw) {
+  const double nmus = double(a.sc_mus);
+  double fx = frag_from_texel_d(ix, (uint32_t)a.W);
+  double f_nu = floor(fx / nmus);
+  double f_mus = fx - nmus * floor(fx / nmus);
+  double x_mu_s = unit_from_coord(f_mus / nmus, a.sc_mus);
+  double d_min = G.T - G.R, d_max = G.H;
   double A = -2.0 * a.mu_s_min * G.R / (d_max - d_min);
   double aa = (A - x_mu_s * A) / (1.0 + x_mu_s * A);
   double d = d_min + gmin(aa, A) * (d_max - d_min);
-  o.mu_s = d == 0.0 ? 1.0 : clamp_cosine((G.H2 - d * d) / (2.0 * G.R * d));
-  double nu = clamp_cosine(qx * 2.0 - 1.0);
+  mu_s = d == 0.0 ? 1.0 : clamp_cosine((G.H2 - d * d) / (2.0 * G.R * d));
+  nu_raw = clamp_cosine(f_nu / double(a.sc_nu - 1) * 2.0 - 1.0);
+}
+__device__ __forceinline__ TexelParams decode_texel64(const DevAtmo& a, const Geo64& G, uint32_t ix, uint32_t iy,
+                                                      uint32_t iz) {
+  TexelParams o;
+  decode_yz64(a, G, iy, iz, o);
+  double nu;
+  decode_x64(a, G, ix, o.mu_s, nu);
   double sq = sqrt((1.0 - o.mu * o.mu) * (1.0 - o.mu_s * o.mu_s));
   o.nu = gclamp(nu, o.mu * o.mu_s - sq, o.mu * o.mu_s + sq);
   return o;

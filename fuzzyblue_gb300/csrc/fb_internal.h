@@ -68,5 +68,8 @@ namespace fbi {
 // The kernels' record of one atmosphere with the default tile shapes (no
 // tables set).
 void fill_atmo_record(fb::DevAtmo& d, const fb_params& p);
+// Points the record's geometry tables at `tp` and advances it past them
+// (the last part of the temporaries, sizes_of(p).tmp_bytes counts them).
+void place_geometry(fb::DevAtmo& d, char*& tp);
 
 }  // namespace fbi

@@ -120,7 +120,7 @@ extern "C" int fb_atmosphere_build_noalloc(void* stream, const fb_params* p, voi
   const fbi::TableSizes z = fbi::sizes_of(*p);
   const bool mixed = p->precision == FB_PRECISION_MIXED;
   const int max_launches = 2 + 2 * 64;
-  const int n_ints = 2 * 2 * max_launches;  // per launch and segment: one job id, one offset
+  const int n_ints = 2 * fb::kMaxSegments * max_launches;  // per launch and segment: one job id, one offset
   size_t off = 0;
   const size_t o_atm = off;
   off = align256(off + sizeof(fb::DevAtmo));
@@ -151,7 +151,11 @@ extern "C" int fb_atmosphere_build_noalloc(void* stream, const fb_params* p, voi
   d.dens = (float4*)tp;    tp += align256(16 * z.nsc);
   if (mixed) {
     d.sc_acc = (double*)tp; tp += align256(24 * z.nsc);
-    d.ir_acc = (double*)tp;
+    d.ir_acc = (double*)tp; tp += align256(24 * z.nir);
+  }
+  {
+    char* gp = (char*)tp;
+    fbi::place_geometry(d, gp);
   }
   // launches of the pass order (src/precompute.rs:1726-1999), one job each
   std::vector<int> ints(n_ints, 0);  // job ids 0, offsets 0
@@ -159,34 +163,39 @@ extern "C" int fb_atmosphere_build_noalloc(void* stream, const fb_params* p, voi
   const int* d_ints = (const int*)(base + o_ints);
   unsigned* d_cnt = (unsigned*)(base + o_cnt);
   std::vector<Launch> L;
-  auto add = [&](int pass, int order, int nseg, int t0, int t1, size_t smem, int tpt) {
+  auto add = [&](int pass, int order, std::vector<int> tiles, size_t smem, int tpt) {
     Launch l;
     std::memset(&l, 0, sizeof(l));
     l.fn = fb::kernel_for(mixed, pass, tpt, 0);
     l.block = pass == fb::kPassDensity ? fb::kDensThreads : fb::kThreads;
     l.smem = smem;
     l.args.atm = d_atm;
-    l.args.nseg = nseg;
+    l.args.nseg = (int)tiles.size();
     l.args.order = order;
     l.args.counter = d_cnt + L.size();
-    const int tiles[2] = {t0, t1};
-    for (int sgi = 0; sgi < nseg; ++sgi) {
+    l.total = 0;
+    for (int sgi = 0; sgi < (int)tiles.size(); ++sgi) {
+      const size_t at = 2 * (fb::kMaxSegments * L.size() + sgi);
       l.args.seg[sgi].njobs = 1;
       l.args.seg[sgi].total = tiles[sgi];
-      l.args.seg[sgi].job = d_ints + 4 * L.size() + 2 * sgi;
-      l.args.seg[sgi].off = d_ints + 4 * L.size() + 2 * sgi + 1;
+      l.args.seg[sgi].job = d_ints + at;
+      l.args.seg[sgi].off = d_ints + at + 1;
+      l.total += tiles[sgi];
     }
-    l.total = t0 + (nseg > 1 ? t1 : 0);
     L.push_back(l);
   };
-  add(fb::kPassTransmittance, 0, 1, fb::tiles_transmittance(d.tr_mu, d.tr_r), 0, 0, 1);
-  add(fb::kPassSingle, 0, 2, fb::tiles_rows(d.W, d.sc_mu, d.sc_r), fb::tiles_direct(d.ir_mus, d.ir_r),
+  const bool multi = d.order >= 2;
+  add(fb::kPassTransmittance, 0,
+      {fb::tiles_transmittance(d.tr_mu, d.tr_r), fb::tiles_geometry(d.W, d.sc_mu, d.sc_r)}, 0, 1);
+  add(fb::kPassSingle, 0,
+      {fb::tiles_rows(d.W, d.sc_mu, d.sc_r), fb::tiles_direct(d.ir_mus, d.ir_r),
+       multi ? fb::tiles_msrec(d.sc_mu, d.sc_r, d.ms_steps) : 0, multi ? fb::tiles_densgeo(d.sc_r, d.dens_n) : 0},
       fb::ss_smem(d.W, d.ss_steps, d.sc_mus, d.sc_nu), 1);
   for (int n = 2; n <= d.order; ++n) {
     const size_t sm = std::max(fb::density_smem(d, n == 2, mixed), fb::indirect_smem(d.irr_n, d.sc_nu, n - 1 == 1));
-    add(fb::kPassDensity, n, 2, fb::tiles_density(d), fb::tiles_indirect(d.ir_mus, d.ir_r), sm, 1);
-    add(fb::kPassMultiple, n, 1, fb::tiles_rows(d.W, d.sc_mu, d.sc_r), 0,
-        fb::ms_smem(d.W, d.ms_steps, d.sc_mus, d.sc_nu), fb::tpt_for_width(d.W));
+    add(fb::kPassDensity, n, {fb::tiles_density(d), fb::tiles_indirect(d.ir_mus, d.ir_r)}, sm, 1);
+    add(fb::kPassMultiple, n, {fb::tiles_rows(d.W, d.sc_mu, d.sc_r)}, fb::ms_smem(d.W, d.ms_steps, d.sc_mus, d.sc_nu),
+        fb::tpt_for_width(d.W));
   }
   cudaError_t e = cudaMemcpyAsync(base + o_atm, &d, sizeof(d), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess)

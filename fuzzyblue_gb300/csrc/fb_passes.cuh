@@ -4,8 +4,11 @@
 //
 // Launch structure (one launch per pass group, any number of atmospheres):
 //   k_transmittance  transmittance.comp                      warp per texel
+//                    geometry tables: rows, x columns (seg 1) thread per entry
 //   k_single         single_scattering.comp  (segment 0)     CTA per (mu, r) row(s)
 //                    direct_irradiance.comp  (segment 1)     thread per texel
+//                    multiple-scattering samples (seg 2)     thread per (row, sample)
+//                    density r / theta records (segment 3)   thread per record
 //   k_density        scattering_density.comp (segment 0)     CTA per (r, mu_s, mu-chunk)
 //                    indirect_irradiance.comp (segment 1)    CTA per texel
 //   k_multiple       multiple_scattering.comp                CTA per (mu, r) row(s)
@@ -29,11 +32,15 @@ struct Segment {
   const int* off;  // first item of each entry (exclusive prefix sum)
 };
 
+constexpr int kMaxSegments = 4;
+
+__host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
 struct LaunchArgs {
   const DevAtmo* atm;
-  Segment seg[2];
+  Segment seg[kMaxSegments];
   int nseg;
-  int order;  // k_density: order n computed (indirect irradiance integrates n-1)
+  int order;  // k_density / k_multiple: order n computed (indirect irradiance integrates n-1)
   unsigned int* counter;
 };
 
@@ -43,21 +50,33 @@ __device__ __forceinline__ bool next_item(const LaunchArgs& L, int& seg, int& jo
   if (threadIdx.x == 0) s_item = (int)atomicAdd(L.counter, 1u);
   __syncthreads();
   int item = s_item;
-  const int total = L.seg[0].total + (L.nseg > 1 ? L.seg[1].total : 0);
-  if (item >= total) return false;
-  seg = 0;
-  if (item >= L.seg[0].total) {
-    seg = 1;
-    item -= L.seg[0].total;
+  // segments are scanned with constant indices so that the launch arguments
+  // stay in parameter space
+  seg = -1;
+  int njobs = 0;
+  const int* jobs = nullptr;
+  const int* offs = nullptr;
+#pragma unroll
+  for (int s = 0; s < kMaxSegments; ++s) {
+    if (seg < 0 && s < L.nseg) {
+      if (item < L.seg[s].total) {
+        seg = s;
+        njobs = L.seg[s].njobs;
+        jobs = L.seg[s].job;
+        offs = L.seg[s].off;
+      } else {
+        item -= L.seg[s].total;
+      }
+    }
   }
-  const Segment& S = L.seg[seg];
-  int lo = 0, hi = S.njobs - 1;
+  if (seg < 0) return false;
+  int lo = 0, hi = njobs - 1;
   while (lo < hi) {
     int mid = (lo + hi + 1) >> 1;
-    if (S.off[mid] <= item) lo = mid; else hi = mid - 1;
+    if (offs[mid] <= item) lo = mid; else hi = mid - 1;
   }
-  job = S.job[lo];
-  tile = item - S.off[lo];
+  job = jobs[lo];
+  tile = item - offs[lo];
   return true;
 }
 
@@ -149,10 +168,6 @@ template <bool MX> __device__ void tile_transmittance(const DevAtmo& a, int tile
   }
 }
 
-template <bool MX> __global__ void __launch_bounds__(kThreads) k_transmittance(LaunchArgs L) {
-  int seg, job, tile;
-  while (next_item(L, seg, job, tile)) tile_transmittance<MX>(L.atm[job], tile);
-}
 
 // =========================================================== S: direct ===
 // direct_irradiance.comp:10-46 plus the clear of the final irradiance table
@@ -191,108 +206,264 @@ template <bool MX> __device__ void tile_direct(const DevAtmo& a, int tile) {
   }
 }
 
-// ===================================================== row-tile helpers ===
-// Single and multiple scattering run one CTA over one or more (mu, r) rows of
-// the packed table: every texel of a row shares r, mu and the ground flag, so
-// the ray geometry of each trapezoid sample is computed once per row.
-struct RowInfo {
-  float r, mu, dx, rr, two_r_mu, r_mu;  // PLAIN: the reference's float values
-  double q, s, dxd, one_m_mu2, mud;     // MIXED: FP64 ray state
-  int ground;
-  int y, z;
-};
-
-template <bool MX> __device__ __forceinline__ void row_info(const DevAtmo& a, int row, int steps, RowInfo& o) {
-  o.y = row % a.sc_mu;
-  o.z = row / a.sc_mu;
-  if (!MX) {
-    Geo32 G;
-    G.init(a);
-    float r, mu, mu_s, nu;
-    bool g;
-    decode_texel32(a, G, 0, (uint32_t)o.y, (uint32_t)o.z, r, mu, mu_s, nu, g);
-    o.r = r;
-    o.mu = mu;
-    o.ground = g;
-    o.dx = (g ? G.dist_bottom(r, mu) : G.dist_top(r, mu)) / float(steps);
-    o.rr = r * r;
-    o.two_r_mu = 2.0f * r * mu;
-    o.r_mu = r * mu;
-  } else {
-    Geo64 G;
-    G.init(a);
-    TexelParams p = decode_texel64(a, G, 0, (uint32_t)o.y, (uint32_t)o.z);
-    o.q = p.q;
-    o.s = p.s;
-    o.r = (float)p.r;
-    o.mu = (float)p.mu;
-    o.ground = p.ground;
-    o.dxd = (p.ground ? G.dist_bottom(p.q, p.s) : G.dist_top(p.q, p.s)) / double(steps);
-    o.dx = (float)o.dxd;
-    o.one_m_mu2 = (1.0 - p.mu) * (1.0 + p.mu);
-    o.mud = p.mu;
+// ============================================================ geometry ===
+// Order-independent tables of one atmosphere (transmittance launch, segment
+// 1): one thread per x column (ColGeo: mu_s and raw nu) and per (mu, r) row
+// (RowGeo: the view ray). PLAIN values are the reference's float decode
+// (scattering.h:62-137), MIXED values its FP64 form.
+template <bool MX> __device__ void tile_geometry(const DevAtmo& a, int tile) {
+  const int k = tile * kThreads + threadIdx.x;
+  const int nrows = a.sc_mu * a.sc_r;
+  if (k < a.W) {
+    ColGeo c;
+    if (!MX) {
+      Geo32 G;
+      G.init(a);
+      decode_x32(a, G, (uint32_t)k, c.mu_s, c.nu_raw);
+      c.one_m_mus2 = 1.0f - c.mu_s * c.mu_s;
+      c.u_mus = G.u_mu_s(a, c.mu_s);
+      c.mu_sd = c.one_m_mus2d = c.nu_rawd = c.t_musd = 0.0;
+    } else {
+      Geo64 G;
+      G.init(a);
+      decode_x64(a, G, (uint32_t)k, c.mu_sd, c.nu_rawd);
+      c.one_m_mus2d = (1.0 - c.mu_sd) * (1.0 + c.mu_sd);
+      c.t_musd = G.mus_unit(a, c.mu_sd) * double(a.sc_mus - 1);
+      c.mu_s = (float)c.mu_sd;
+      c.one_m_mus2 = (float)c.one_m_mus2d;
+      c.nu_raw = (float)c.nu_rawd;
+      c.u_mus = 0.f;
+    }
+    a.g_cols[k] = c;
+  } else if (k < a.W + nrows) {
+    const int row = k - a.W;
+    const uint32_t y = (uint32_t)(row % a.sc_mu), z = (uint32_t)(row / a.sc_mu);
+    RowGeo o;
+    o.pad = 0;
+    if (!MX) {
+      Geo32 G;
+      G.init(a);
+      float r, mu;
+      bool g;
+      decode_yz32(a, G, y, z, r, mu, g);
+      o.r = r;
+      o.mu = mu;
+      o.ground = g;
+      o.dist = g ? G.dist_bottom(r, mu) : G.dist_top(r, mu);
+      o.rr = r * r;
+      o.two_r_mu = 2.0f * r * mu;
+      o.r_mu = r * mu;
+      o.q = o.s = o.distd = o.one_m_mu2 = o.mud = 0.0;
+    } else {
+      Geo64 G;
+      G.init(a);
+      TexelParams p;
+      decode_yz64(a, G, y, z, p);
+      o.q = p.q;
+      o.s = p.s;
+      o.r = (float)p.r;
+      o.mu = (float)p.mu;
+      o.ground = p.ground;
+      o.distd = p.ground ? G.dist_bottom(p.q, p.s) : G.dist_top(p.q, p.s);
+      o.dist = (float)o.distd;
+      o.one_m_mu2 = (1.0 - p.mu) * (1.0 + p.mu);
+      o.mud = p.mu;
+      o.rr = o.two_r_mu = o.r_mu = 0.f;
+    }
+    a.g_rows[row] = o;
   }
 }
 
-// MIXED: FP64 decode of the mu_s coordinate (scattering.h:102-111) and of the
-// raw nu coordinate (scattering.h:113), tabulated per column class.
-__device__ __forceinline__ void decode_mus_nu64(const DevAtmo& a, const Geo64& G, int x, double& mu_s,
-                                                double& nu_raw) {
-  const double nmus = double(a.sc_mus);
-  double fx = frag_from_texel_d((uint32_t)x, (uint32_t)a.W);
-  double f_nu = floor(fx / nmus);
-  double f_mus = fx - nmus * floor(fx / nmus);
-  double x_mu_s = unit_from_coord(f_mus / nmus, a.sc_mus);
-  double d_min = G.T - G.R, d_max = G.H;
-  double A = -2.0 * a.mu_s_min * G.R / (d_max - d_min);
-  double aa = (A - x_mu_s * A) / (1.0 + x_mu_s * A);
-  double d = d_min + gmin(aa, A) * (d_max - d_min);
-  mu_s = d == 0.0 ? 1.0 : clamp_cosine((G.H2 - d * d) / (2.0 * G.R * d));
-  nu_raw = clamp_cosine(f_nu / double(a.sc_nu - 1) * 2.0 - 1.0);
+__host__ __device__ inline int tiles_geometry(int W, int sc_mu, int sc_r) {
+  return (W + sc_mu * sc_r + kThreads - 1) / kThreads;
 }
 
-// Column tables of a row tile (MIXED only): mu_s and 1 - mu_s^2 per mu_s index,
-// raw nu per nu index.
-struct ColTabs {
-  double2* mus;  // sc_mus entries: (mu_s, 1 - mu_s^2)
-  double* nu;    // sc_nu entries: raw nu
-};
-__device__ __forceinline__ void build_cols(const DevAtmo& a, ColTabs c) {
-  Geo64 G;
-  G.init(a);
-  for (int k = threadIdx.x; k < a.sc_mus + a.sc_nu; k += kThreads) {
-    double mu_s, nu;
-    if (k < a.sc_mus) {
-      decode_mus_nu64(a, G, k, mu_s, nu);
-      c.mus[k] = make_double2(mu_s, (1.0 - mu_s) * (1.0 + mu_s));
-    } else {
-      const int n = k - a.sc_mus;
-      decode_mus_nu64(a, G, n * a.sc_mus, mu_s, nu);
-      c.nu[n] = nu;
-    }
+template <bool MX> __global__ void __launch_bounds__(kThreads) k_transmittance(LaunchArgs L) {
+  int seg, job, tile;
+  while (next_item(L, seg, job, tile)) {
+    if (seg == 0) tile_transmittance<MX>(L.atm[job], tile);
+    else tile_geometry<MX>(L.atm[job], tile);
   }
 }
 
 // mu_s, nu (clamped to the range allowed by mu and mu_s, scattering.h:134-136)
-// and r*mu_s of texel x of a row.
+// and r * mu_s of texel x of a row, from the geometry tables.
 template <bool MX>
-__device__ __forceinline__ void texel_mus_nu(const DevAtmo& a, const RowInfo& ri, const ColTabs& c, int x,
-                                             float& mu_s, float& nu, float& r_mu_s) {
+__device__ __forceinline__ void texel_mus_nu(const RowGeo& ri, const ColGeo& c, float& mu_s, float& nu,
+                                             float& r_mu_s) {
+  mu_s = c.mu_s;
+  if (!MX) {
+    nu = clamp_nu32(c.nu_raw, ri.mu, mu_s, c.one_m_mus2);
+  } else {
+    // 1 - mu^2 and 1 - mu_s^2 come from FP64 without cancellation; nothing
+    // downstream of nu cancels, so the clamp runs in FP32.
+    const float sq = sqrtf((float)ri.one_m_mu2 * c.one_m_mus2), mm = ri.mu * mu_s;
+    nu = mm + gclamp(c.nu_raw - mm, -sq, sq);
+  }
+  r_mu_s = ri.r * mu_s;
+}
+
+__host__ __device__ inline int rows_per_tile(int W) { return W >= kThreads ? 1 : kThreads / W; }
+
+// ======================================================= MS sample records ===
+// multiple_scattering.comp:19-40, the parts that depend on the view ray and
+// the sample only (single-scattering launch, segment 2): the sample distance
+// and radius, the transmittance from the texel times dx and the trapezoid
+// weight, and the (mu, r) sampler axes of the density lookup.
+template <bool MX> __device__ void tile_msrec(const DevAtmo& a, int tile) {
+  const int NS = a.ms_steps + 1;
+  const int k = tile * kThreads + threadIdx.x;
+  const int nrows = a.sc_mu * a.sc_r;
+  if (k >= nrows * NS) return;
+  const int row = k / NS, i = k % NS, N = a.ms_steps;
+  const RowGeo ri = a.g_rows[row];
+  MSRec o;
+  o.pad = 0;
+  const float w = (i == 0 || i == N) ? 0.5f : 1.0f;
+  float3 tv;
+  Axis ay, az;
+  float dx;
+  if (!MX) {
+    Geo32 G;
+    G.init(a);
+    dx = ri.dist / float(N);
+    const float d = float(i) * dx;
+    const float r_i = G.clamp_radius(sqrtf(d * d + ri.two_r_mu * d + ri.rr));
+    const float mu_i = clamp_cosine((ri.r_mu + d) / r_i);
+    tv = G.tr_segment(a, ri.r, ri.mu, d, ri.ground);
+    az = make_axis(G.u_r(a, r_i), a.sc_r);
+    ay = make_axis(G.u_mu(a, r_i, mu_i, ri.ground), a.sc_mu);
+    o.d = d;
+    o.inv_r = 1.0f / r_i;
+  } else {
+    GeoMx G;
+    G.init(a);
+    const double dxd = ri.distd / double(N);
+    dx = (float)dxd;
+    const double d = double(i) * dxd;
+    double q = fma(d, 2.0 * ri.s + d, ri.q), sd = ri.s + d;
+    q = fmin(fmax(q, 0.0), G.H2);
+    const float r_i = sqrtf((float)q + G.R * G.R);
+    sd = fmin(fmax(sd, -(double)r_i), (double)r_i);
+    tv = G.tr_segment(a, ri.q, ri.s, d, ri.ground);
+    az = axis_texel(G.sc_r_texel(q), a.sc_r);
+    ay = axis_texel(G.sc_mu_texel(q, sd, ri.ground), a.sc_mu);
+    o.d = (float)d;
+    o.inv_r = 1.0f / r_i;
+  }
+  const float wdx = dx * w;
+  o.tvwx = tv.x * wdx;
+  o.tvwy = tv.y * wdx;
+  o.tvwz = tv.z * wdx;
+  o.y0 = ay.i0;
+  o.y1 = ay.i1;
+  o.fy = ay.f;
+  o.z0 = az.i0;
+  o.z1 = az.i1;
+  o.fz = az.f;
+  a.g_ms[k] = o;
+}
+
+__host__ __device__ inline int tiles_msrec(int sc_mu, int sc_r, int ms_steps) {
+  return (sc_mu * sc_r * (ms_steps + 1) + kThreads - 1) / kThreads;
+}
+
+// =================================================== density r / theta ===
+// scattering_density.comp:36-60, the parts that depend on r and the theta
+// row only (single-scattering launch, segment 3): per r slice the r axis of
+// the 3D tables; per (r slice, theta row) the direction's cosine, the solid
+// angle of its row, the ground hit (distance, transmittance x albedo / pi)
+// and the mu axis of the lookup.
+template <bool MX> __device__ void tile_densgeo(const DevAtmo& a, int tile) {
+  const int NT = a.dens_n;
+  const int k = tile * kThreads + threadIdx.x;
+  if (k >= a.sc_r * (NT + 1)) return;
+  if (k < a.sc_r) {
+    DensZ o;
+    o.pad = 0;
+    if (!MX) {
+      Geo32 G;
+      G.init(a);
+      float r, mu;
+      bool g;
+      decode_yz32(a, G, 0u, (uint32_t)k, r, mu, g);
+      o.r = r;
+      o.q = 0.0;
+      o.az = make_axis(G.u_r(a, r), a.sc_r);
+      // irradiance at the ground: irradiance.h:20-30 with r = bottom (x_r = 0)
+      o.irx = make_axis(coord_from_unit((a.bottom - a.bottom) / (a.top - a.bottom), a.ir_r), a.ir_r);
+    } else {
+      Geo64 G;
+      G.init(a);
+      TexelParams tp;
+      decode_yz64(a, G, 0u, (uint32_t)k, tp);
+      o.r = (float)tp.r;
+      o.q = tp.q;
+      o.az = axis_texel(G.sc_r_texel(a, tp.q), a.sc_r);
+      o.irx = axis_texel(0.0f, a.ir_r);
+    }
+    a.g_z[k] = o;
+    return;
+  }
+  const int zi = (k - a.sc_r) / NT, l = (k - a.sc_r) % NT;
+  ThetaRec out;
+  out.pad = 0;
+  DensTheta& o = out.th;
+  o.pad = 0;
   if (!MX) {
     Geo32 G;
     G.init(a);
     float r, mu;
-    bool g;
-    decode_texel32(a, G, (uint32_t)x, (uint32_t)ri.y, (uint32_t)ri.z, r, mu, mu_s, nu, g);
-    r_mu_s = ri.r * mu_s;
+    bool gg;
+    decode_yz32(a, G, 0u, (uint32_t)zi, r, mu, gg);
+    const float dtheta = kPiF / float(NT), dphi = kPiF / float(NT);
+    const float theta = (float(l) + 0.5f) * dtheta;
+    const float ct = cosf(theta);
+    const bool g = G.hits_ground(r, ct);
+    float3 tg = make_float3(0.f, 0.f, 0.f);
+    float dg = 0.0f;
+    if (g) {
+      dg = G.dist_bottom(r, ct);
+      tg = G.tr_segment(a, r, ct, dg, true) * ld3(a.albedo) * (1.0f / kPiF);
+    }
+    o.cos_t = ct;
+    o.domega = dtheta * dphi * sinf(theta);
+    o.dg = dg;
+    o.ground = g;
+    o.tgx = tg.x;
+    o.tgy = tg.y;
+    o.tgz = tg.z;
+    out.tay = make_axis(G.u_mu(a, r, ct, g), a.sc_mu);
   } else {
-    // the clamp in FP64 (scattering.h:134-136)
-    const double2 ms = c.mus[x % a.sc_mus];
-    const double sq = sqrt(ri.one_m_mu2 * ms.y), mm = ri.mud * ms.x;
-    mu_s = (float)ms.x;
-    nu = (float)(mm + gclamp(c.nu[x / a.sc_mus] - mm, -sq, sq));
-    r_mu_s = ri.r * mu_s;
+    Geo64 G;
+    G.init(a);
+    TexelParams tp;
+    decode_yz64(a, G, 0u, (uint32_t)zi, tp);
+    const double dtheta = kPiD / double(NT), dphi = kPiD / double(NT);
+    const double theta = (double(l) + 0.5) * dtheta;
+    const double ct = cos(theta);
+    const double q = tp.q, sv = G.radius(q) * ct;
+    const bool g = G.hits_ground(q, sv);
+    float3 tg = make_float3(0.f, 0.f, 0.f);
+    double dg = 0.0;
+    if (g) {
+      dg = G.dist_bottom(q, sv);
+      tg = G.tr_segment(a, q, sv, dg, true) * ld3(a.albedo) * (float)(1.0 / kPiD);
+    }
+    o.cos_t = (float)ct;
+    o.domega = (float)(dtheta * dphi * sin(theta));
+    o.dg = (float)dg;
+    o.ground = g;
+    o.tgx = tg.x;
+    o.tgy = tg.y;
+    o.tgz = tg.z;
+    out.tay = axis_texel(G.sc_mu_texel(a, q, sv, g), a.sc_mu);
   }
+  a.g_th[zi * NT + l] = out;
+}
+
+__host__ __device__ inline int tiles_densgeo(int sc_r, int dens_n) {
+  return (sc_r * (dens_n + 1) + kThreads - 1) / kThreads;
 }
 
 // ============================================================ S: single ===
@@ -301,7 +472,6 @@ struct SSRec {
   int y0, y1;
 };
 
-__host__ __device__ inline int rows_per_tile(int W) { return W >= kThreads ? 1 : kThreads / W; }
 
 template <bool MX>
 __device__ void tile_single(const DevAtmo& a, int tile, unsigned char* smem) {
@@ -310,19 +480,15 @@ __device__ void tile_single(const DevAtmo& a, int tile, unsigned char* smem) {
   const int row0 = tile * R;
   const int nrow = min(R, nrows - row0);
   const int N = a.ss_steps, NS = N + 1;
-  RowInfo* rows = (RowInfo*)smem;
-  SSRec* rec = (SSRec*)(rows + R);
-  ColTabs cols;
-  cols.mus = (double2*)(((uintptr_t)(rec + (size_t)R * NS) + 15) & ~(uintptr_t)15);
-  cols.nu = (double*)(cols.mus + a.sc_mus);
+  RowGeo* rows = (RowGeo*)smem;
+  SSRec* rec = (SSRec*)(smem + align16(sizeof(RowGeo) * R));
   const int tid = threadIdx.x;
-  if (tid < nrow) row_info<MX>(a, row0 + tid, N, rows[tid]);
-  if (MX) build_cols(a, cols);
+  if (tid < nrow) rows[tid] = a.g_rows[row0 + tid];
   __syncthreads();
   // Per (row, sample): the view ray point, the transmittance to it, the
   // densities there and the parts of the sun lookup that depend on it only.
   for (int k = tid; k < nrow * NS; k += kThreads) {
-    const RowInfo& ri = rows[k / NS];
+    const RowGeo& ri = rows[k / NS];
     const int i = k % NS;
     SSRec& o = rec[k];
     o.w = (i == 0 || i == N) ? 0.5f : 1.0f;
@@ -332,7 +498,8 @@ __device__ void tile_single(const DevAtmo& a, int tile, unsigned char* smem) {
       G.init(a);
       float v;
       // single_scattering.comp:16-23
-      float d = float(i) * ri.dx;
+      const float dx = ri.dist / float(N);
+      float d = float(i) * dx;
       float r_d = G.clamp_radius(sqrtf(d * d + ri.two_r_mu * d + ri.rr));
       tv = G.tr_segment(a, ri.r, ri.mu, d, ri.ground);
       o.d = d;
@@ -359,7 +526,7 @@ __device__ void tile_single(const DevAtmo& a, int tile, unsigned char* smem) {
     } else {
       GeoMx G;
       G.init(a);
-      const double d = double(i) * ri.dxd;
+      const double d = double(i) * (ri.distd / double(N));
       double q = fma(d, 2.0 * ri.s + d, ri.q);
       q = fmin(fmax(q, 0.0), G.H2);
       const float qf = (float)q;
@@ -395,9 +562,9 @@ __device__ void tile_single(const DevAtmo& a, int tile, unsigned char* smem) {
   const float trc0 = 0.5f / float(a.tr_mu), trc1 = 1.0f - 1.0f / float(a.tr_mu), trn = float(a.tr_mu);
   for (int k = tid; k < nrow * W; k += kThreads) {
     const int lr = k / W, x = k % W;
-    const RowInfo& ri = rows[lr];
+    const RowGeo& ri = rows[lr];
     float mu_s, nu, r_mu_s;
-    texel_mus_nu<MX>(a, ri, cols, x, mu_s, nu, r_mu_s);
+    texel_mus_nu<MX>(ri, a.g_cols[x], mu_s, nu, r_mu_s);
     const SSRec* rr = rec + lr * NS;
     Kahan3 ray, mie;
     ray.init();
@@ -440,7 +607,7 @@ __device__ void tile_single(const DevAtmo& a, int tile, unsigned char* smem) {
         mie.add(mi_ * o.w);
       }
     }
-    const float dx = ri.dx;
+    const float dx = MX ? (float)(ri.distd / double(N)) : ri.dist / float(N);
     const float3 rs = MX ? make_float3(ray.s.x - ray.c.x, ray.s.y - ray.c.y, ray.s.z - ray.c.z) : ray.s;
     const float3 ms = MX ? make_float3(mie.s.x - mie.c.x, mie.s.y - mie.c.y, mie.s.z - mie.c.z) : mie.s;
     const float3 R3 = rs * dx * ld3(a.solar) * ld3(a.rayleigh);
@@ -462,7 +629,9 @@ template <bool MX> __global__ void __launch_bounds__(kThreads) k_single(LaunchAr
   int seg, job, tile;
   while (next_item(L, seg, job, tile)) {
     if (seg == 0) tile_single<MX>(L.atm[job], tile, smem);
-    else tile_direct<MX>(L.atm[job], tile);
+    else if (seg == 1) tile_direct<MX>(L.atm[job], tile);
+    else if (seg == 2) tile_msrec<MX>(L.atm[job], tile);
+    else tile_densgeo<MX>(L.atm[job], tile);
   }
 }
 
@@ -482,11 +651,6 @@ template <bool MX> __global__ void __launch_bounds__(kThreads) k_single(LaunchAr
 //    component), so each pair shares one phase evaluation.
 constexpr int kDensThreads = 128;
 constexpr int kDensMaxGroup = 8;
-
-struct DensTheta {
-  float cos_t, domega, dg, tgx, tgy, tgz;
-  int ground, pad;
-};
 
 // Per-atmosphere tile shape of the density pass (host and device agree).
 struct DensShape {
@@ -535,7 +699,6 @@ struct DensLayout {
   float* acc;       // kDensThreads * kDensMaxGroup * 3 * 2 (MIXED: Kahan sum over theta rows)
 };
 
-__host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
 __host__ __device__ inline size_t dens_layout(unsigned char* base, int dens_n, int sc_nu, int ir_mus, int S,
                                               int chunk, bool two, bool mixed, DensLayout* L) {
@@ -597,116 +760,34 @@ __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned cha
   DensLayout S;
   dens_layout(smem, NT, NNU, a.ir_mus, sh.S, sh.chunk, two, MX, &S);
 
-  __shared__ Axis s_az, s_irx;
-  __shared__ float s_r;
-  __shared__ double s_q;
-  // --- tile scalars: r and its axis (z); the ground irradiance row axis
-  if (tid == 0) {
-    if (!MX) {
-      Geo32 G;
-      G.init(a);
-      float r, mu, mu_s, nu;
-      bool g;
-      decode_texel32(a, G, (uint32_t)s0, 0u, (uint32_t)zi, r, mu, mu_s, nu, g);
-      s_r = r;
-      s_az = make_axis(G.u_r(a, r), a.sc_r);
-      // irradiance at the ground: irradiance.h:20-30 with r = bottom (x_r = 0)
-      s_irx = make_axis(coord_from_unit((a.bottom - a.bottom) / (a.top - a.bottom), a.ir_r), a.ir_r);
-    } else {
-      Geo64 G;
-      G.init(a);
-      TexelParams tp = decode_texel64(a, G, (uint32_t)s0, 0u, (uint32_t)zi);
-      s_r = (float)tp.r;
-      s_q = tp.q;
-      s_az = axis_texel(G.sc_r_texel(a, tp.q), a.sc_r);
-      s_irx = axis_texel(0.0f, a.ir_r);
-    }
-  }
-  __syncthreads();
-  const float r = s_r;
-  // --- per theta, per column, per mu row / nu (MIXED decode tables)
+  // --- tile scalars (r slice), theta rows, columns and mu rows from the
+  // geometry tables
+  const DensZ zr = a.g_z[zi];
+  const float r = zr.r;
+  const Axis s_az = zr.az, s_irx = zr.irx;
+  const ThetaRec* thr = a.g_th + (size_t)zi * NT;
   for (int k = tid; k < NT + ns + (MX ? ny + NNU : 0); k += nth) {
     if (k < NT) {
-      const int l = k;
-      DensTheta& o = S.th[l];
-      if (!MX) {
-        Geo32 G;
-        G.init(a);
-        const float dtheta = kPiF / float(NT), dphi = kPiF / float(NT);
-        const float theta = (float(l) + 0.5f) * dtheta;
-        const float ct = cosf(theta);
-        const bool g = G.hits_ground(r, ct);
-        float3 tg = make_float3(0.f, 0.f, 0.f);
-        float dg = 0.0f;
-        if (g) {
-          dg = G.dist_bottom(r, ct);
-          tg = G.tr_segment(a, r, ct, dg, true) * ld3(a.albedo) * (1.0f / kPiF);
-        }
-        o.cos_t = ct;
-        o.domega = dtheta * dphi * sinf(theta);
-        o.dg = dg;
-        o.ground = g;
-        o.tgx = tg.x;
-        o.tgy = tg.y;
-        o.tgz = tg.z;
-        S.tay[l] = make_axis(G.u_mu(a, r, ct, g), a.sc_mu);
-      } else {
-        Geo64 G;
-        G.init(a);
-        const double dtheta = kPiD / double(NT), dphi = kPiD / double(NT);
-        const double theta = (double(l) + 0.5) * dtheta;
-        const double ct = cos(theta);
-        const double q = s_q, sv = G.radius(q) * ct;
-        const bool g = G.hits_ground(q, sv);
-        float3 tg = make_float3(0.f, 0.f, 0.f);
-        double dg = 0.0;
-        if (g) {
-          dg = G.dist_bottom(q, sv);
-          tg = G.tr_segment(a, q, sv, dg, true) * ld3(a.albedo) * (float)(1.0 / kPiD);
-        }
-        o.cos_t = (float)ct;
-        o.domega = (float)(dtheta * dphi * sin(theta));
-        o.dg = (float)dg;
-        o.ground = g;
-        o.tgx = tg.x;
-        o.tgy = tg.y;
-        o.tgz = tg.z;
-        S.tay[l] = axis_texel(G.sc_mu_texel(a, q, sv, g), a.sc_mu);
-      }
+      const ThetaRec t = thr[k];
+      S.th[k] = t.th;
+      S.tay[k] = t.tay;
     } else if (k < NT + ns) {
       const int c = k - NT, si = s0 + c;
+      const ColGeo cg = a.g_cols[si];
+      S.col_mus[c] = cg.mu_s;
       if (!MX) {
-        Geo32 G;
-        G.init(a);
-        float rr, mu, mu_s, nu;
-        bool g;
-        decode_texel32(a, G, (uint32_t)si, 0u, (uint32_t)zi, rr, mu, mu_s, nu, g);
-        S.col_mus[c] = mu_s;
-        const float u_ms = G.u_mu_s(a, mu_s);
-        for (int j = 0; j < NK; ++j) S.kax[c * NK + j] = make_axis((float(j - 1) + u_ms) / float(NNU), a.W);
+        for (int j = 0; j < NK; ++j) S.kax[c * NK + j] = make_axis((float(j - 1) + cg.u_mus) / float(NNU), a.W);
       } else {
-        Geo64 G;
-        G.init(a);
-        double mu_s, nu;
-        decode_mus_nu64(a, G, si, mu_s, nu);
-        S.col_mus[c] = (float)mu_s;
-        S.col_musd[c] = mu_s;
-        const double y = G.mus_unit(a, mu_s);
-        for (int j = 0; j < NK; ++j)
-          S.kax[c * NK + j] = axis_texel(double(j - 1) * a.sc_mus + y * double(a.sc_mus - 1), a.W);
+        S.col_musd[c] = cg.mu_sd;
+        for (int j = 0; j < NK; ++j) S.kax[c * NK + j] = axis_texel(double(j - 1) * a.sc_mus + cg.t_musd, a.W);
       }
     } else if (MX) {
-      Geo64 G;
-      G.init(a);
       const int k2 = k - NT - ns;
       if (k2 < ny) {
-        TexelParams tp = decode_texel64(a, G, (uint32_t)s0, (uint32_t)(y0 + k2), (uint32_t)zi);
-        S.ymu[k2] = make_double2(tp.mu, (1.0 - tp.mu) * (1.0 + tp.mu));
+        const RowGeo& rg = a.g_rows[zi * a.sc_mu + y0 + k2];
+        S.ymu[k2] = make_double2(rg.mud, rg.one_m_mu2);
       } else {
-        const int n = k2 - ny;
-        double mu_s, nu;
-        decode_mus_nu64(a, G, n * a.sc_mus, mu_s, nu);
-        S.nuraw[n] = nu;
+        S.nuraw[k2 - ny] = a.g_cols[(k2 - ny) * a.sc_mus].nu_rawd;
       }
     }
   }
@@ -785,11 +866,9 @@ __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned cha
       if (j < G) {
         const int nu_i = grp * G + j, x = nu_i * a.sc_mus + si;
         if (!MX) {
-          Geo32 Gm;
-          Gm.init(a);
-          float rr, ms, nu;
-          bool gg;
-          decode_texel32(a, Gm, (uint32_t)x, (uint32_t)y, (uint32_t)zi, rr, mu, ms, nu, gg);
+          mu = a.g_rows[zi * a.sc_mu + y].mu;
+          const ColGeo& cg = a.g_cols[x];
+          const float ms = cg.mu_s, nu = clamp_nu32(cg.nu_raw, mu, ms, cg.one_m_mus2);
           // scattering_density.comp:28-32
           ox = sqrtf(1.0f - mu * mu);
           sx[j] = ox == 0.0f ? 0.0f : (nu - mu * ms) / ox;
@@ -1076,87 +1155,40 @@ template <bool MX, int V> __global__ void __launch_bounds__(kDensThreads, V == 0
 // multiple_scattering.comp:9-93. Every texel of a row shares the ray (r, mu)
 // and hence, for each trapezoid sample, the sample radius, its mu, the
 // transmittance from the texel and the (mu, r) coordinates of the density
-// lookup. For each sample the CTA interpolates the density table in (mu, r)
-// once into a slab over x; each texel then blends four slab entries (two
-// mu_s neighbours in two nu slices).
-struct MSRec {
-  float d, inv_r, wdx, tvx, tvy, tvz, fy, fz;
-  int y0, y1, z0, z1;
-};
-
+// lookup: those come from the sample records (MSRec) computed once per build.
+// For each sample the CTA interpolates the density table in (mu, r) once into
+// a slab over x; each texel then blends four slab entries (two mu_s
+// neighbours in two nu slices).
 __host__ __device__ inline size_t ms_smem(int W, int steps, int sc_mus, int sc_nu) {
+  (void)sc_mus;
+  (void)sc_nu;
   const int R = rows_per_tile(W);
-  return align16(sizeof(RowInfo) * R) + align16(sizeof(MSRec) * (size_t)R * (steps + 1)) +
-         2 * sizeof(float4) * (size_t)R * W + align16(sizeof(double2) * sc_mus) + align16(sizeof(double) * sc_nu);
+  return align16(sizeof(MSRec) * (size_t)R * (steps + 1)) + 2 * sizeof(float4) * (size_t)R * W;
 }
 
 template <bool MX, int TPT>
-__device__ void tile_multiple(const DevAtmo& a, int tile, unsigned char* smem) {
+__device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned char* smem) {
   const int W = a.W, nrows = a.sc_mu * a.sc_r;
   const int R = rows_per_tile(W);
   const int row0 = tile * R;
   const int nrow = min(R, nrows - row0);
   const int N = a.ms_steps, NS = N + 1;
   const int tid = threadIdx.x;
-  unsigned char* p = smem;
-  RowInfo* rows = (RowInfo*)p;                 p += align16(sizeof(RowInfo) * R);
-  MSRec* rec = (MSRec*)p;                      p += align16(sizeof(MSRec) * (size_t)R * NS);
-  float4* slab = (float4*)p;                   p += 2 * sizeof(float4) * (size_t)R * W;
-  ColTabs cols;
-  cols.mus = (double2*)p;                      p += align16(sizeof(double2) * a.sc_mus);
-  cols.nu = (double*)p;
+  MSRec* rec = (MSRec*)smem;
+  float4* slab = (float4*)(smem + align16(sizeof(MSRec) * (size_t)R * NS));
   const int slab_n = nrow * W;
   const int slab_stride = R * W;
-  if (tid < nrow) row_info<MX>(a, row0 + tid, N, rows[tid]);
-  if (MX) build_cols(a, cols);
-  __syncthreads();
-  for (int k = tid; k < nrow * NS; k += kThreads) {
-    const RowInfo& ri = rows[k / NS];
-    const int i = k % NS;
-    MSRec& o = rec[k];
-    const float w = (i == 0 || i == N) ? 0.5f : 1.0f;
-    float3 tv;
-    Axis ay, az;
-    if (!MX) {
-      Geo32 G;
-      G.init(a);
-      const float d = float(i) * ri.dx;
-      const float r_i = G.clamp_radius(sqrtf(d * d + ri.two_r_mu * d + ri.rr));
-      const float mu_i = clamp_cosine((ri.r_mu + d) / r_i);
-      tv = G.tr_segment(a, ri.r, ri.mu, d, ri.ground);
-      az = make_axis(G.u_r(a, r_i), a.sc_r);
-      ay = make_axis(G.u_mu(a, r_i, mu_i, ri.ground), a.sc_mu);
-      o.d = d;
-      o.inv_r = 1.0f / r_i;
-    } else {
-      GeoMx G;
-      G.init(a);
-      const double d = double(i) * ri.dxd;
-      double q = fma(d, 2.0 * ri.s + d, ri.q), s = ri.s + d;
-      q = fmin(fmax(q, 0.0), G.H2);
-      const float r_i = sqrtf((float)q + G.R * G.R);
-      s = fmin(fmax(s, -(double)r_i), (double)r_i);
-      tv = G.tr_segment(a, ri.q, ri.s, d, ri.ground);
-      az = axis_texel(G.sc_r_texel(q), a.sc_r);
-      ay = axis_texel(G.sc_mu_texel(q, s, ri.ground), a.sc_mu);
-      o.d = (float)d;
-      o.inv_r = 1.0f / r_i;
-    }
-    o.wdx = ri.dx * w;
-    o.tvx = tv.x;
-    o.tvy = tv.y;
-    o.tvz = tv.z;
-    o.y0 = ay.i0;
-    o.y1 = ay.i1;
-    o.fy = ay.f;
-    o.z0 = az.i0;
-    o.z1 = az.i1;
-    o.fz = az.f;
+  {  // this tile's sample records
+    const int4* src = reinterpret_cast<const int4*>(a.g_ms + (size_t)row0 * NS);
+    int4* dst = reinterpret_cast<int4*>(rec);
+    const int n16 = nrow * NS * (int)(sizeof(MSRec) / sizeof(int4));
+    for (int k = tid; k < n16; k += kThreads) dst[k] = __ldg(src + k);
   }
-  __syncthreads();
   // per-texel constants (TPT texels per thread)
   float c_rmus[TPT], c_nu[TPT], c_lerp[TPT], c_tex[TPT];
+  int c_lr[TPT], c_x[TPT];
   Kahan3 acc[TPT];
+  float3 part[TPT];
   MuS32 mus32;
   mus32.init(a);
   MuSRef32 musref;
@@ -1164,12 +1196,14 @@ __device__ void tile_multiple(const DevAtmo& a, int tile, unsigned char* smem) {
 #pragma unroll
   for (int j = 0; j < TPT; ++j) {
     acc[j].init();
+    part[j] = make_float3(0.f, 0.f, 0.f);
     c_rmus[j] = c_nu[j] = c_lerp[j] = c_tex[j] = 0.f;
     const int k = tid + j * kThreads;
+    c_lr[j] = k / W;
+    c_x[j] = k - c_lr[j] * W;
     if (k < slab_n) {
-      const int lr = k / W, x = k % W;
       float mu_s, nu, rmus;
-      texel_mus_nu<MX>(a, rows[lr], cols, x, mu_s, nu, rmus);
+      texel_mus_nu<MX>(a.g_rows[row0 + c_lr[j]], a.g_cols[c_x[j]], mu_s, nu, rmus);
       c_nu[j] = nu;
       c_rmus[j] = rmus;
       // scattering.h:146-148
@@ -1179,6 +1213,7 @@ __device__ void tile_multiple(const DevAtmo& a, int tile, unsigned char* smem) {
       c_tex[j] = fl;
     }
   }
+  __syncthreads();
   const float4* dens = a.dens;
   const size_t plane = (size_t)a.sc_mu * W;
   // Slab of sample i: the density table interpolated in (mu, r) at the
@@ -1187,14 +1222,14 @@ __device__ void tile_multiple(const DevAtmo& a, int tile, unsigned char* smem) {
   auto load = [&](int i) {
 #pragma unroll
     for (int j = 0; j < TPT; ++j) {
-      const int k = tid + j * kThreads;
-      if (k < slab_n) {
-        const int lr = k / W, x = k % W;
-        const MSRec& o = rec[lr * NS + i];
-        nx[j][0] = ld4(dens + o.z0 * plane + (size_t)o.y0 * W + x);
-        nx[j][1] = ld4(dens + o.z0 * plane + (size_t)o.y1 * W + x);
-        nx[j][2] = ld4(dens + o.z1 * plane + (size_t)o.y0 * W + x);
-        nx[j][3] = ld4(dens + o.z1 * plane + (size_t)o.y1 * W + x);
+      if (tid + j * kThreads < slab_n) {
+        const MSRec& o = rec[c_lr[j] * NS + i];
+        const float4* p0 = dens + o.z0 * plane + c_x[j];
+        const float4* p1 = dens + o.z1 * plane + c_x[j];
+        nx[j][0] = ld4(p0 + (size_t)o.y0 * W);
+        nx[j][1] = ld4(p0 + (size_t)o.y1 * W);
+        nx[j][2] = ld4(p1 + (size_t)o.y0 * W);
+        nx[j][3] = ld4(p1 + (size_t)o.y1 * W);
       }
     }
   };
@@ -1203,7 +1238,7 @@ __device__ void tile_multiple(const DevAtmo& a, int tile, unsigned char* smem) {
     for (int j = 0; j < TPT; ++j) {
       const int k = tid + j * kThreads;
       if (k < slab_n) {
-        const MSRec& o = rec[(k / W) * NS + i];
+        const MSRec& o = rec[c_lr[j] * NS + i];
         const float w00 = (1.f - o.fy) * (1.f - o.fz), w10 = o.fy * (1.f - o.fz);
         const float w01 = (1.f - o.fy) * o.fz, w11 = o.fy * o.fz;
         const float4 a00 = nx[j][0], a10 = nx[j][1], a01 = nx[j][2], a11 = nx[j][3];
@@ -1222,16 +1257,10 @@ __device__ void tile_multiple(const DevAtmo& a, int tile, unsigned char* smem) {
   const float fmus = float(a.sc_mus);
   for (int i = 0; i < NS; ++i) {
     const float4* cur = slab + (i & 1) * slab_stride;
-    // the next sample's rows load after this sample's arithmetic: holding them
-    // across it costs more occupancy than the overlap gains
-    constexpr bool kPrefetch = false;
-    if (kPrefetch && i + 1 < NS) load(i + 1);
 #pragma unroll
     for (int j = 0; j < TPT; ++j) {
-      const int k = tid + j * kThreads;
-      if (k < slab_n) {
-        const int lr = k / W;
-        const MSRec& o = rec[lr * NS + i];
+      if (tid + j * kThreads < slab_n) {
+        const MSRec& o = rec[c_lr[j] * NS + i];
         const float nu = c_nu[j];
         const float tx = c_tex[j];
         Axis x0, x1;
@@ -1248,20 +1277,28 @@ __device__ void tile_multiple(const DevAtmo& a, int tile, unsigned char* smem) {
           x0 = axis_texel(fmaf(tx, fmus, t), W);
           x1 = axis_texel(fmaf(tx + 1.0f, fmus, t), W);
         }
-        const float4* sl = cur + lr * W;
+        const float4* sl = cur + c_lr[j] * W;
         const float4 p00 = sl[x0.i0], p01 = sl[x0.i1], p10 = sl[x1.i0], p11 = sl[x1.i1];
         const float lf = c_lerp[j];
         const float ax = fmaf(p01.x - p00.x, x0.f, p00.x), bx = fmaf(p11.x - p10.x, x1.f, p10.x);
         const float ay = fmaf(p01.y - p00.y, x0.f, p00.y), by = fmaf(p11.y - p10.y, x1.f, p10.y);
         const float az = fmaf(p01.z - p00.z, x0.f, p00.z), bz = fmaf(p11.z - p10.z, x1.f, p10.z);
         const float3 J = make_float3(fmaf(bx - ax, lf, ax), fmaf(by - ay, lf, ay), fmaf(bz - az, lf, az));
-        const float3 v = J * make_float3(o.tvx, o.tvy, o.tvz) * o.wdx;
-        if (!MX) acc[j].s = acc[j].s + v;
-        else acc[j].add(v);
+        const float3 v = J * make_float3(o.tvwx, o.tvwy, o.tvwz);
+        if (!MX) {
+          acc[j].s = acc[j].s + v;
+        } else {
+          // plain sums over runs of 8 samples, Kahan-compensated across runs
+          part[j] = part[j] + v;
+          if ((i & 7) == 7 || i == N) {
+            acc[j].add(part[j]);
+            part[j] = make_float3(0.f, 0.f, 0.f);
+          }
+        }
       }
     }
     if (i + 1 < NS) {
-      if (!kPrefetch) load(i + 1);
+      load(i + 1);
       store(i + 1, slab + ((i + 1) & 1) * slab_stride);
     }
     __syncthreads();
@@ -1271,22 +1308,27 @@ __device__ void tile_multiple(const DevAtmo& a, int tile, unsigned char* smem) {
   for (int j = 0; j < TPT; ++j) {
     const int k = tid + j * kThreads;
     if (k < slab_n) {
-      const int lr = k / W, x = k % W;
-      const size_t t = (size_t)(row0 + lr) * W + x;
+      const size_t t = (size_t)(row0 + c_lr[j]) * W + c_x[j];
       const float3 ms = make_float3(acc[j].s.x - acc[j].c.x, acc[j].s.y - acc[j].c.y, acc[j].s.z - acc[j].c.z);
       a.dms[t] = store_round4(make_float4(ms.x, ms.y, ms.z, 0.f), a.f16);
       const float pr = phase_rayleigh(c_nu[j]);
-      const float4 old = a.sc[t];
       if (!MX) {
+        const float4 old = a.sc[t];
         a.sc[t] = store_round4(make_float4(ms.x / pr + old.x, ms.y / pr + old.y, ms.z / pr + old.z, 0.f + old.w),
                                a.f16);
       } else {
+        // orders accumulate in FP64; the FP32 table is written after the last
         double* s3 = a.sc_acc + 3 * t;
         const float ipr = 1.0f / pr;
-        s3[0] += (double)(ms.x * ipr);
-        s3[1] += (double)(ms.y * ipr);
-        s3[2] += (double)(ms.z * ipr);
-        a.sc[t] = store_round4(make_float4((float)s3[0], (float)s3[1], (float)s3[2], old.w), a.f16);
+        const double sx = s3[0] + (double)(ms.x * ipr), sy = s3[1] + (double)(ms.y * ipr),
+                     sz = s3[2] + (double)(ms.z * ipr);
+        s3[0] = sx;
+        s3[1] = sy;
+        s3[2] = sz;
+        if (order == a.order) {
+          const float w = a.sc[t].w;
+          a.sc[t] = store_round4(make_float4((float)sx, (float)sy, (float)sz, w), a.f16);
+        }
       }
     }
   }
@@ -1298,7 +1340,7 @@ template <bool MX, int TPT, int V>
 __global__ void __launch_bounds__(kThreads, TPT <= 2 ? (V == 0 ? 4 : 3) : (V == 0 ? 2 : 1)) k_multiple(LaunchArgs L) {
   extern __shared__ __align__(16) unsigned char smem[];
   int seg, job, tile;
-  while (next_item(L, seg, job, tile)) tile_multiple<MX, TPT>(L.atm[job], tile, smem);
+  while (next_item(L, seg, job, tile)) tile_multiple<MX, TPT>(L.atm[job], L.order, tile, smem);
 }
 
 // ------------------------------------------------------ tile geometry ----
@@ -1316,9 +1358,10 @@ __host__ __device__ inline int tiles_density(const DevAtmo& a) {
   return dens_shape(a.sc_r, a.sc_mu, a.sc_mus, a.sc_nu, a.dens_S, a.dens_chunk).tiles;
 }
 __host__ __device__ inline size_t ss_smem(int W, int steps, int sc_mus, int sc_nu) {
+  (void)sc_mus;
+  (void)sc_nu;
   const int R = rows_per_tile(W);
-  return sizeof(RowInfo) * R + sizeof(SSRec) * (size_t)R * (steps + 1) + 16 + sizeof(double2) * sc_mus +
-         sizeof(double) * sc_nu + 16;
+  return align16(sizeof(RowGeo) * R) + sizeof(SSRec) * (size_t)R * (steps + 1);
 }
 __host__ __device__ inline size_t density_smem(const DevAtmo& a, bool two, bool mixed) {
   const DensShape d = dens_shape(a.sc_r, a.sc_mu, a.sc_mus, a.sc_nu, a.dens_S, a.dens_chunk);
