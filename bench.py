@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--batch", type=int, default=BATCH)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "plain"],
+                    help="arithmetic of the batch (the headline is mixed)")
     return ap.parse_args()
 
 
@@ -188,11 +190,12 @@ def run_ours(a):
         td.init_process_group("nccl")
     from fuzzyblue_gb300 import workloads
     from fuzzyblue_gb300.api import Atmosphere, Builder, build_batch
-    from fuzzyblue_gb300.params import Parameters
+    from fuzzyblue_gb300.params import PRECISION_MIXED, PRECISION_PLAIN, Parameters
 
     builder = Builder(local)
     stream = torch.cuda.Stream()
-    params = workloads.uniform_batch(a.batch, seed=0, order=ORDERS)
+    prec = PRECISION_MIXED if a.precision == "mixed" else PRECISION_PLAIN
+    params = workloads.uniform_batch(a.batch, seed=0, order=ORDERS, precision=prec)
 
     def step(profile=False):
         builder.set_profiling(profile)
@@ -220,6 +223,7 @@ def run_ours(a):
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     step_ms, prof = [], []
     ev0.record(stream)
+    torch.cuda.nvtx.range_push("timed")  # lets a profiler select the timed launches
     for _ in range(a.steps):
         s0 = torch.cuda.Event(enable_timing=True)
         s1 = torch.cuda.Event(enable_timing=True)
@@ -230,6 +234,7 @@ def run_ours(a):
         prof.append(p.profile())
         p.release()
         step_ms.append(s0.elapsed_time(s1))
+    torch.cuda.nvtx.range_pop()
     ev1.record(stream)
     torch.cuda.synchronize()
     barrier(world)
@@ -310,7 +315,8 @@ def run_ours(a):
     peaks = measured_peaks()
 
     out = {
-        "metric": METRIC,
+        "metric": METRIC if a.precision == "mixed" else METRIC.replace(
+            "mixed precision (<=1e-3 rel err vs FP64)", "plain FP32"),
         "value": value,
         "unit": "atmospheres/s",
         "n_gpus": world,
@@ -320,9 +326,10 @@ def run_ours(a):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32 with f64 ray geometry and order accumulation",
+        "dtype": "f32 with f64 ray geometry and order accumulation" if a.precision == "mixed" else "f32",
         "data": "synthetic: seeded atmospheres (fuzzyblue_gb300.workloads, seed 0)",
-        "config": {"workload": WORKLOAD, "batch_per_gpu": a.batch, "orders": ORDERS, "precision": "mixed",
+        "config": {"workload": WORKLOAD if a.precision == "mixed" else WORKLOAD.replace("mixed", "plain FP32"),
+                   "batch_per_gpu": a.batch, "orders": ORDERS, "precision": a.precision,
                    "parallelism": "replicas" if world > 1 else "single",
                    "l2": "inputs larger than L2: ~%d GB of tables and temporaries per step" % round(
                        a.batch * 0.1)},

@@ -257,7 +257,7 @@ extern "C" int fb_builder_create(int device, fb_builder** out) {
   cudaDeviceProp prop;
   FB_CU(cudaGetDeviceProperties(&prop, device));
   cudaFuncAttributes fa;
-  if (cudaFuncGetAttributes(&fa, fb::kernel_plain(fb::kPassDensity, 1, 0)) != cudaSuccess) {
+  if (cudaFuncGetAttributes(&fa, fb::kernel_plain(fb::kPassDensity, 1, 0, false)) != cudaSuccess) {
     cudaGetLastError();
     return fail(FB_ERR_NO_KERNEL, "no sm_103a kernel image loads on device %d (%s, sm_%d%d)", device, prop.name,
                 prop.major, prop.minor);
@@ -288,8 +288,8 @@ extern "C" int fb_builder_create(int device, fb_builder** out) {
   for (int mode = 0; mode < 2; ++mode)
     for (int pass = 0; pass < 4; ++pass)
       for (int tpt : {1, 2, 4, 8})
-        for (int variant : {0, 1}) {
-        const void* k = fb::kernel_for(mode == 1, pass, tpt, variant);
+        for (int variant : {0, 1, 2, 3}) {
+        const void* k = fb::kernel_for(mode == 1, pass, tpt, variant & 1, variant >= 2);
         cudaFuncAttributes kfa;
         if (cudaFuncGetAttributes(&kfa, k) != cudaSuccess ||
             cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -740,7 +740,7 @@ int build(fb_builder* b, cudaStream_t s, const fb_params* params, uint32_t count
   for (size_t li = 0; li < plan.launches.size(); ++li) {
     const PlannedLaunch& L = plan.launches[li];
     Ready R;
-    R.fn = fb::kernel_for(L.mixed, L.pass, L.tpt, L.variant);
+    R.fn = fb::kernel_for(L.mixed, L.pass, L.tpt, L.variant, L.order == 2);
     R.smem = L.smem;
     cudaFuncAttributes kfa;
     if (cudaFuncGetAttributes(&kfa, R.fn) != cudaSuccess) return bail(FB_ERR_CUDA, "cudaFuncGetAttributes failed");

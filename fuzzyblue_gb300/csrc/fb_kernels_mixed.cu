@@ -6,8 +6,10 @@ namespace fb {
 
 template __global__ void k_transmittance<true>(LaunchArgs);
 template __global__ void k_single<true>(LaunchArgs);
-template __global__ void k_density<true, 0>(LaunchArgs);
-template __global__ void k_density<true, 1>(LaunchArgs);
+template __global__ void k_density<true, 0, false>(LaunchArgs);
+template __global__ void k_density<true, 1, false>(LaunchArgs);
+template __global__ void k_density<true, 0, true>(LaunchArgs);
+template __global__ void k_density<true, 1, true>(LaunchArgs);
 template __global__ void k_multiple<true, 1, 0>(LaunchArgs);
 template __global__ void k_multiple<true, 2, 0>(LaunchArgs);
 template __global__ void k_multiple<true, 4, 0>(LaunchArgs);
@@ -17,12 +19,14 @@ template __global__ void k_multiple<true, 2, 1>(LaunchArgs);
 template __global__ void k_multiple<true, 4, 1>(LaunchArgs);
 template __global__ void k_multiple<true, 8, 1>(LaunchArgs);
 
-const void* kernel_mixed(int pass, int tpt, int variant) {
+const void* kernel_mixed(int pass, int tpt, int variant, bool order2) {
   const bool v1 = variant == 1;
   switch (pass) {
     case kPassTransmittance: return (const void*)k_transmittance<true>;
     case kPassSingle: return (const void*)k_single<true>;
-    case kPassDensity: return v1 ? (const void*)k_density<true, 1> : (const void*)k_density<true, 0>;
+    case kPassDensity:
+      if (order2) return v1 ? (const void*)k_density<true, 1, true> : (const void*)k_density<true, 0, true>;
+      return v1 ? (const void*)k_density<true, 1, false> : (const void*)k_density<true, 0, false>;
     case kPassMultiple:
       switch (tpt) {
         case 1: return v1 ? (const void*)k_multiple<true, 1, 1> : (const void*)k_multiple<true, 1, 0>;

@@ -7,8 +7,10 @@ namespace fb {
 
 template __global__ void k_transmittance<false>(LaunchArgs);
 template __global__ void k_single<false>(LaunchArgs);
-template __global__ void k_density<false, 0>(LaunchArgs);
-template __global__ void k_density<false, 1>(LaunchArgs);
+template __global__ void k_density<false, 0, false>(LaunchArgs);
+template __global__ void k_density<false, 1, false>(LaunchArgs);
+template __global__ void k_density<false, 0, true>(LaunchArgs);
+template __global__ void k_density<false, 1, true>(LaunchArgs);
 template __global__ void k_multiple<false, 1, 0>(LaunchArgs);
 template __global__ void k_multiple<false, 2, 0>(LaunchArgs);
 template __global__ void k_multiple<false, 4, 0>(LaunchArgs);
@@ -18,12 +20,14 @@ template __global__ void k_multiple<false, 2, 1>(LaunchArgs);
 template __global__ void k_multiple<false, 4, 1>(LaunchArgs);
 template __global__ void k_multiple<false, 8, 1>(LaunchArgs);
 
-const void* kernel_plain(int pass, int tpt, int variant) {
+const void* kernel_plain(int pass, int tpt, int variant, bool order2) {
   const bool v1 = variant == 1;
   switch (pass) {
     case kPassTransmittance: return (const void*)k_transmittance<false>;
     case kPassSingle: return (const void*)k_single<false>;
-    case kPassDensity: return v1 ? (const void*)k_density<false, 1> : (const void*)k_density<false, 0>;
+    case kPassDensity:
+      if (order2) return v1 ? (const void*)k_density<false, 1, true> : (const void*)k_density<false, 0, true>;
+      return v1 ? (const void*)k_density<false, 1, false> : (const void*)k_density<false, 0, false>;
     case kPassMultiple:
       switch (tpt) {
         case 1: return v1 ? (const void*)k_multiple<false, 1, 1> : (const void*)k_multiple<false, 1, 0>;

@@ -69,8 +69,9 @@ int setup_device(int dev, DeviceSetup** out) {
     }
     for (int mode = 0; mode < 2; ++mode)
       for (int pass = 0; pass < 4; ++pass)
-        for (int tpt : {1, 2, 4, 8}) {
-          const void* k = fb::kernel_for(mode == 1, pass, tpt, 0);
+        for (int tpt : {1, 2, 4, 8})
+          for (int order2 = 0; order2 < 2; ++order2) {
+          const void* k = fb::kernel_for(mode == 1, pass, tpt, 0, order2 == 1);
           cudaFuncAttributes fa;
           if (cudaFuncGetAttributes(&fa, k) != cudaSuccess ||
               cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -166,7 +167,7 @@ extern "C" int fb_atmosphere_build_noalloc(void* stream, const fb_params* p, voi
   auto add = [&](int pass, int order, std::vector<int> tiles, size_t smem, int tpt) {
     Launch l;
     std::memset(&l, 0, sizeof(l));
-    l.fn = fb::kernel_for(mixed, pass, tpt, 0);
+    l.fn = fb::kernel_for(mixed, pass, tpt, 0, order == 2);
     l.block = pass == fb::kPassDensity ? fb::kDensThreads : fb::kThreads;
     l.smem = smem;
     l.args.atm = d_atm;

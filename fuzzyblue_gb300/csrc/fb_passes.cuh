@@ -136,17 +136,19 @@ template <bool MX> __device__ void tile_transmittance(const DevAtmo& a, int tile
     double d = d_min + x_mu * (d_max - d_min);
     double s = d == 0.0 ? r : gclamp((G.H2 - q - d * d) / (2.0 * d), -r, r);
     const double dx = G.dist_top(q, s) / double(N);
-    const double two_s = 2.0 * s, R2 = G.R * G.R;
-    const float Rf = a.bottom;
+    // The march runs in FP32 on the FP64 ray state (q, 2 s, dx): r_k^2 - R^2 =
+    // q + d_k (2 s + d_k) keeps the altitude q_k / (r_k + R) free of the
+    // cancellation of r_k - R, to ~1e-5 km where the ray grazes the ground.
+    const float qf = (float)q, two_sf = (float)(2.0 * s), dxf = (float)dx, Rf = a.bottom, R2f = Rf * Rf;
     float cR = 0.f, cM = 0.f, cA = 0.f;
     sR = sM = sA = 0.0f;
     for (int k = lane; k <= N; k += 32) {
-      double d_k = double(k) * dx;
-      double q_k = fma(d_k, two_s + d_k, q);  // r_k^2 - R^2, no cancellation
-      float r_k = sqrtf((float)(q_k + R2));
+      const float d_k = float(k) * dxf;
+      const float q_k = fmaf(d_k, two_sf + d_k, qf);
+      const float r_k = sqrtf(q_k + R2f);
       // every ray of this table stays at or above the ground: a negative
       // altitude here is rounding at a tangent sample
-      float h = gmax((float)q_k / (r_k + Rf), 0.0f);
+      float h = gmax(__fdividef(q_k, r_k + Rf), 0.0f);
       float w = (k == 0 || k == N) ? 0.5f : 1.0f;
       Kahan3::add1(sR, cR, profile_density(a.ray_d, h) * w);
       Kahan3::add1(sM, cM, profile_density(a.mie_d, h) * w);
@@ -684,14 +686,23 @@ __host__ __device__ inline DensShape dens_shape(int sc_r, int sc_mu, int sc_mus,
   return d;
 }
 
+// An entry of a linearly interpolated RGB table: value in a.xyz, difference to
+// the next entry in (a.w, b.x, b.y); 32 bytes, read as one 16- and one 8-byte
+// load from the same base address.
+struct LerpRec {
+  float4 a;
+  float2 b;
+  float2 pad;
+};
+
 struct DensLayout {
   DensTheta* th;    // NT
   Axis* tay;        // NT: theta -> mu axis
   Axis* kax;        // S * NK: (column, nu slice) -> x axis
   float4* dir;      // NT * NT mirror pairs: (cos phi sin t, sin phi sin t, ground normal x, y)
   float* gnz;       // NT * NT: ground normal z
-  float4* P;        // S * NT * NK * 2 float4 per table (value.rgb + dx, dy dz)
-  float4* irow;     // ir_mus: ground irradiance row (the two sampler rows pre-blended)
+  LerpRec* P;       // per table, S * NT * NK: value rgb and delta to the next nu slice
+  LerpRec* E;       // ir_mus: ground irradiance row (the two sampler rows pre-blended) and delta
   float* col_mus;   // S
   double* col_musd; // S (MIXED)
   double2* ymu;     // chunk (MIXED): (mu, 1 - mu^2)
@@ -699,10 +710,10 @@ struct DensLayout {
   float* acc;       // kDensThreads * kDensMaxGroup * 3 * 2 (MIXED: Kahan sum over theta rows)
 };
 
-
 __host__ __device__ inline size_t dens_layout(unsigned char* base, int dens_n, int sc_nu, int ir_mus, int S,
                                               int chunk, bool two, bool mixed, DensLayout* L) {
   const int NT = dens_n, NK = sc_nu + 2;
+  const size_t nP = (size_t)S * NT * NK * (two ? 2 : 1);
   size_t o = 0;
   auto take = [&](size_t bytes) {
     size_t at = o;
@@ -711,8 +722,7 @@ __host__ __device__ inline size_t dens_layout(unsigned char* base, int dens_n, i
   };
   size_t o_th = take(sizeof(DensTheta) * NT), o_tay = take(sizeof(Axis) * NT), o_kax = take(sizeof(Axis) * S * NK);
   size_t o_dir = take(sizeof(float4) * NT * NT), o_gnz = take(sizeof(float) * NT * NT);
-  size_t o_P = take(sizeof(float4) * 2 * (size_t)S * NT * NK * (two ? 2 : 1));
-  size_t o_irow = take(sizeof(float4) * ir_mus);
+  size_t o_P = take(sizeof(LerpRec) * nP), o_E = take(sizeof(LerpRec) * ir_mus);
   size_t o_cm = take(sizeof(float) * S), o_cmd = take(sizeof(double) * S);
   size_t o_ymu = take(mixed ? sizeof(double2) * chunk : 0), o_nu = take(mixed ? sizeof(double) * sc_nu : 0);
   size_t o_acc = take(mixed ? sizeof(float) * kDensThreads * kDensMaxGroup * 6 : 0);
@@ -722,8 +732,8 @@ __host__ __device__ inline size_t dens_layout(unsigned char* base, int dens_n, i
     L->kax = (Axis*)(base + o_kax);
     L->dir = (float4*)(base + o_dir);
     L->gnz = (float*)(base + o_gnz);
-    L->P = (float4*)(base + o_P);
-    L->irow = (float4*)(base + o_irow);
+    L->P = (LerpRec*)(base + o_P);
+    L->E = (LerpRec*)(base + o_E);
     L->col_mus = (float*)(base + o_cm);
     L->col_musd = (double*)(base + o_cmd);
     L->ymu = (double2*)(base + o_ymu);
@@ -747,7 +757,86 @@ struct PhaseCoef {
   }
 };
 
-template <bool MX>
+// Linear interpolation position in a table of n entries for a cosine c in
+// [-1, 1] (texel coordinate (c + 1) / 2 (n - 1), the sampler's u n - 1/2 for
+// u = coord_from_unit((c + 1) / 2)): entry k in [0, n - 2] and weight f in
+// [0, 1] of entry k + 1. Rounding (t - 1/2) to an integer through the float
+// adder (adding 1.5 * 2^23) gives floor(t), or floor(t) - 1 with f = 1 where t
+// is an integer: the same interpolated value. The saturation clamps rounding
+// excursions of c beyond [-1, 1], so k never leaves the table.
+constexpr float kRoundMagic = 12582912.0f;  // 1.5 * 2^23
+constexpr int kRoundMagicBits = 0x4B400000;
+__device__ __forceinline__ int lerp_pos(float c, float n_minus_1, float& f) {
+  const float u = __saturatef(fmaf(c, 0.5f, 0.5f));
+  const float y = fmaf(u, n_minus_1, -0.5f) + kRoundMagic;
+  f = fmaf(u, n_minus_1, -(y - kRoundMagic));
+  return __float_as_int(y) - kRoundMagicBits;
+}
+
+// The directions of one theta row for the G texels of a thread (all sharing
+// r, mu and mu_s): incident radiance of order n - 1 from the reduced table
+// (scattering.h:139-179), plus for rows that meet the ground the ground
+// bounce (scattering_density.comp:64-84), times the phase functions
+// (scattering_density.comp:86-104).
+template <bool TWO, bool GROUND>
+__device__ __forceinline__ void dens_row(const DensLayout& S, const DensTheta& t, int l, int NT,
+                                         const LerpRec* __restrict__ Pl, const LerpRec* __restrict__ Ml, float mu,
+                                         float mu_s, float ox, const float (&sx)[kDensMaxGroup],
+                                         const float (&sy)[kDensMaxGroup], int G, const PhaseCoef& pc, float kray,
+                                         float kmie, float nu_n1, float ir_n1, float3 (&acc)[kDensMaxGroup]) {
+  const float mus_ct = mu_s * t.cos_t, mu_ct = mu * t.cos_t;
+  const float4* dirl = S.dir + l * NT;
+  const float* gnzl = S.gnz + l * NT;
+  for (int m = 0; m < NT; ++m) {
+    const float4 d = dirl[m];
+    // phase functions of omega . omega_i, shared by the pair and the group
+    const float nu2 = fmaf(ox, d.x, mu_ct);
+    const float3 cf = pc.eval(nu2, t.domega);
+    const float gzm = GROUND ? gnzl[m] * mu_s : 0.f;
+#pragma unroll
+    for (int j = 0; j < kDensMaxGroup; ++j) {
+      if (j < G) {
+        const float base = fmaf(sx[j], d.x, mus_ct), dy = sy[j] * d.y;
+        const float gb = GROUND ? fmaf(d.z, sx[j], gzm) : 0.f, gdy = GROUND ? d.w * sy[j] : 0.f;
+#pragma unroll
+        for (int side = 0; side < 2; ++side) {
+          const float nu1 = side ? base - dy : base + dy;
+          float lf;
+          const int k = lerp_pos(nu1, nu_n1, lf);
+          const float4 pa = Pl[k].a;
+          const float2 pb = Pl[k].b;
+          float3 inc = make_float3(fmaf(pa.w, lf, pa.x), fmaf(pb.x, lf, pa.y), fmaf(pb.y, lf, pa.z));
+          if (TWO) {
+            const float4 qa = Ml[k].a;
+            const float2 qb = Ml[k].b;
+            const float pr = kray * fmaf(nu1, nu1, 1.0f);
+            const float rs = rsqrtf(fmaf(-pc.g2, nu1, pc.g1));
+            const float pm = kmie * fmaf(nu1, nu1, 1.0f) * (rs * rs * rs);
+            inc.x = fmaf(fmaf(qa.w, lf, qa.x), pm, inc.x * pr);
+            inc.y = fmaf(fmaf(qb.x, lf, qa.y), pm, inc.y * pr);
+            inc.z = fmaf(fmaf(qb.y, lf, qa.z), pm, inc.z * pr);
+          }
+          if (GROUND) {
+            // irradiance of order n - 2 where omega_i meets the ground
+            const float mg = side ? gb - gdy : gb + gdy;
+            float lg;
+            const int e = lerp_pos(mg, ir_n1, lg);
+            const float4 ea = S.E[e].a;
+            const float2 eb = S.E[e].b;
+            inc.x = fmaf(t.tgx, fmaf(ea.w, lg, ea.x), inc.x);
+            inc.y = fmaf(t.tgy, fmaf(eb.x, lg, ea.y), inc.y);
+            inc.z = fmaf(t.tgz, fmaf(eb.y, lg, ea.z), inc.z);
+          }
+          acc[j].x = fmaf(inc.x, cf.x, acc[j].x);
+          acc[j].y = fmaf(inc.y, cf.y, acc[j].y);
+          acc[j].z = fmaf(inc.z, cf.z, acc[j].z);
+        }
+      }
+    }
+  }
+}
+
+template <bool MX, bool TWO>
 __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned char* smem) {
   const int NT = a.dens_n, NNU = a.sc_nu, NK = NNU + 2;
   const DensShape sh = dens_shape(a.sc_r, a.sc_mu, a.sc_mus, a.sc_nu, a.dens_S, a.dens_chunk);
@@ -755,10 +844,9 @@ __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned cha
   const int rem = tile % (sh.scols * sh.ychunks);
   const int s0 = (rem / sh.ychunks) * sh.S, y0 = (rem % sh.ychunks) * sh.chunk;
   const int ns = min(sh.S, a.sc_mus - s0), ny = min(sh.chunk, a.sc_mu - y0);
-  const bool two = (order - 1) == 1;  // order 2 reads the single Rayleigh/Mie tables
   const int tid = threadIdx.x, nth = blockDim.x;
   DensLayout S;
-  dens_layout(smem, NT, NNU, a.ir_mus, sh.S, sh.chunk, two, MX, &S);
+  dens_layout(smem, NT, NNU, a.ir_mus, sh.S, sh.chunk, TWO, MX, &S);
 
   // --- tile scalars (r slice), theta rows, columns and mu rows from the
   // geometry tables
@@ -792,23 +880,20 @@ __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned cha
     }
   }
   __syncthreads();
-  // --- reduced tables, direction pairs with ground normals, ground irradiance row
+  // --- reduced tables: the previous order's table at this tile's r and mu_s
+  // columns, on the theta rows, per nu slice (values first, then deltas to the
+  // next slice); direction pairs with ground normals; ground irradiance row
+  const size_t nPtab = (size_t)sh.S * NT * NK;
+  const int per_col = NT * NK;
   {
-    const float4* src0 = two ? a.dr : a.dms;
-    const int per_col = NT * NK;
+    const float4* src0 = TWO ? a.dr : a.dms;
     for (int k = tid; k < ns * per_col; k += nth) {
       const int c = k / per_col, l = (k % per_col) / NK, sl = k % NK;
-      const int slc = min(sl + 1, NK - 1);
-      const float3 v0 = fetch3(src0, a.W, a.sc_mu, S.kax[c * NK + sl], S.tay[l], s_az);
-      const float3 v1 = sl + 1 < NK ? fetch3(src0, a.W, a.sc_mu, S.kax[c * NK + slc], S.tay[l], s_az) : v0;
-      S.P[2 * k] = make_float4(v0.x, v0.y, v0.z, v1.x - v0.x);
-      S.P[2 * k + 1] = make_float4(v1.y - v0.y, v1.z - v0.z, 0.f, 0.f);
-      if (two) {
-        const float3 m0 = fetch3(a.dm, a.W, a.sc_mu, S.kax[c * NK + sl], S.tay[l], s_az);
-        const float3 m1 = sl + 1 < NK ? fetch3(a.dm, a.W, a.sc_mu, S.kax[c * NK + slc], S.tay[l], s_az) : m0;
-        const size_t off = 2 * (size_t)sh.S * per_col;
-        S.P[off + 2 * k] = make_float4(m0.x, m0.y, m0.z, m1.x - m0.x);
-        S.P[off + 2 * k + 1] = make_float4(m1.y - m0.y, m1.z - m0.z, 0.f, 0.f);
+      const float3 v = fetch3(src0, a.W, a.sc_mu, S.kax[c * NK + sl], S.tay[l], s_az);
+      S.P[k].a = make_float4(v.x, v.y, v.z, 0.f);
+      if (TWO) {
+        const float3 m = fetch3(a.dm, a.W, a.sc_mu, S.kax[c * NK + sl], S.tay[l], s_az);
+        S.P[nPtab + k].a = make_float4(m.x, m.y, m.z, 0.f);
       }
     }
     const float dtheta = kPiF / float(NT), dphi = kPiF / float(NT);
@@ -828,8 +913,25 @@ __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned cha
     const float fy = s_irx.f;
     for (int k = tid; k < a.ir_mus; k += nth) {
       const float4 e0 = E[s_irx.i0 * a.ir_mus + k], e1 = E[s_irx.i1 * a.ir_mus + k];
-      S.irow[k] = make_float4(fmaf(e1.x - e0.x, fy, e0.x), fmaf(e1.y - e0.y, fy, e0.y), fmaf(e1.z - e0.z, fy, e0.z),
-                              0.f);
+      S.E[k].a = make_float4(fmaf(e1.x - e0.x, fy, e0.x), fmaf(e1.y - e0.y, fy, e0.y), fmaf(e1.z - e0.z, fy, e0.z),
+                             0.f);
+    }
+  }
+  __syncthreads();
+  {  // deltas to the next slice / irradiance entry
+    for (int k = tid; k < ns * per_col; k += nth) {
+      const bool last = (k % NK) == NK - 1;
+      for (int tb = 0; tb < (TWO ? 2 : 1); ++tb) {
+        const size_t o = tb * nPtab + k;
+        const float4 v0 = S.P[o].a, v1 = last ? v0 : S.P[o + 1].a;
+        S.P[o].b = make_float2(v1.y - v0.y, v1.z - v0.z);
+        S.P[o].a.w = v1.x - v0.x;
+      }
+    }
+    for (int k = tid; k < a.ir_mus; k += nth) {
+      const float4 v0 = S.E[k].a, v1 = k + 1 < a.ir_mus ? S.E[k + 1].a : v0;
+      S.E[k].b = make_float2(v1.y - v0.y, v1.z - v0.z);
+      S.E[k].a.w = v1.x - v0.x;
     }
   }
   __syncthreads();
@@ -896,81 +998,34 @@ __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned cha
     pc.B = make_float3(a.mie_sca[0] * rho_m * kmie, a.mie_sca[1] * rho_m * kmie, a.mie_sca[2] * rho_m * kmie);
     pc.g1 = 1.0f + g * g;
     pc.g2 = 2.0f * g;
-    const float hf = 0.5f * float(NNU - 1);
-    const float fmaxk = float(NNU - 1);
-    // ground irradiance row coordinate: u = coord(mg / 2 + 1/2), texel u n - 1/2
-    const float ir_c0 = 0.5f / float(a.ir_mus), ir_c1 = 1.0f - 1.0f / float(a.ir_mus), ir_n = float(a.ir_mus);
+    const float nu_n1 = float(NNU - 1), ir_n1 = float(a.ir_mus - 1);
     float3 acc[kDensMaxGroup];
 #pragma unroll
     for (int j = 0; j < kDensMaxGroup; ++j) acc[j] = make_float3(0.f, 0.f, 0.f);
-    float* accs = S.acc + (size_t)tid * kDensMaxGroup * 6;  // (sum, compensation) x 3 x G
+    // (sum, compensation) x 3 x G per thread, element e at accs[e * kDensThreads]:
+    // consecutive threads use consecutive banks, offsets are immediates
+    float* accs = S.acc + tid;
     if (MX) {
-      for (int j = 0; j < 6 * kDensMaxGroup; ++j) accs[j] = 0.f;
+#pragma unroll
+      for (int e = 0; e < 6 * kDensMaxGroup; ++e) accs[e * kDensThreads] = 0.f;
     }
-    const size_t ptab = 2 * (size_t)sh.S * NT * NK;
     for (int l = 0; l < NT; ++l) {
       const DensTheta t = S.th[l];
-      const float mus_ct = mu_s * t.cos_t, mu_ct = mu * t.cos_t;
-      const float4* Pl = S.P + 2 * (size_t)((cl * NT + l) * NK);
-      const float4* Ml = Pl + ptab;
-      for (int m = 0; m < NT; ++m) {
-        const float4 d = S.dir[l * NT + m];
-        // phase functions of omega . omega_i, shared by the pair and the group
-        const float nu2 = fmaf(ox, d.x, mu_ct);
-        const float3 cf = pc.eval(nu2, t.domega);
-        const float gzm = t.ground ? S.gnz[l * NT + m] * mu_s : 0.f;
-#pragma unroll
-        for (int j = 0; j < kDensMaxGroup; ++j) {
-          if (j < G) {
-            const float base = fmaf(sx[j], d.x, mus_ct), dy = sy[j] * d.y;
-            const float gb = fmaf(d.z, sx[j], gzm), gdy = d.w * sy[j];
-#pragma unroll
-            for (int side = 0; side < 2; ++side) {
-              // incident radiance of order n-1 (scattering.h:139-179)
-              const float nu1 = side ? base - dy : base + dy;
-              const float tcx = fmaf(nu1, hf, hf);
-              float fk = floorf(tcx);
-              const float lf = tcx - fk;
-              fk = fminf(fmaxf(fk, -1.0f), fmaxk);
-              const int ks = 2 * ((int)fk + 1);
-              const float4 p0 = Pl[ks], p1 = Pl[ks + 1];
-              float3 inc = make_float3(fmaf(p0.w, lf, p0.x), fmaf(p1.x, lf, p0.y), fmaf(p1.y, lf, p0.z));
-              if (two) {
-                const float4 q0 = Ml[ks], q1 = Ml[ks + 1];
-                const float pr = kray * fmaf(nu1, nu1, 1.0f);
-                const float rs = rsqrtf(fmaf(-pc.g2, nu1, pc.g1));
-                const float pm = kmie * fmaf(nu1, nu1, 1.0f) * (rs * rs * rs);
-                inc.x = fmaf(fmaf(q0.w, lf, q0.x), pm, inc.x * pr);
-                inc.y = fmaf(fmaf(q1.x, lf, q0.y), pm, inc.y * pr);
-                inc.z = fmaf(fmaf(q1.y, lf, q0.z), pm, inc.z * pr);
-              }
-              if (t.ground) {
-                // ground bounce: irradiance of order n-2 where omega_i meets the ground
-                const float mg = side ? gb - gdy : gb + gdy;
-                float tx;
-                if (!MX) tx = fmaf(fmaf(fmaf(mg, 0.5f, 0.5f), ir_c1, ir_c0), ir_n, -0.5f);
-                else tx = fmaf(mg, 0.5f, 0.5f) * float(a.ir_mus - 1);
-                const Axis ax = axis_texel(tx, a.ir_mus);
-                const float4 e0 = S.irow[ax.i0], e1 = S.irow[ax.i1];
-                inc.x = fmaf(t.tgx, fmaf(e1.x - e0.x, ax.f, e0.x), inc.x);
-                inc.y = fmaf(t.tgy, fmaf(e1.y - e0.y, ax.f, e0.y), inc.y);
-                inc.z = fmaf(t.tgz, fmaf(e1.z - e0.z, ax.f, e0.z), inc.z);
-              }
-              acc[j].x = fmaf(inc.x, cf.x, acc[j].x);
-              acc[j].y = fmaf(inc.y, cf.y, acc[j].y);
-              acc[j].z = fmaf(inc.z, cf.z, acc[j].z);
-            }
-          }
-        }
-      }
+      // +1: the reduced table starts at nu slice -1
+      const LerpRec* Pl = S.P + (size_t)(cl * NT + l) * NK + 1;
+      const LerpRec* Ml = Pl + nPtab;
+      if (t.ground)
+        dens_row<TWO, true>(S, t, l, NT, Pl, Ml, mu, mu_s, ox, sx, sy, G, pc, kray, kmie, nu_n1, ir_n1, acc);
+      else
+        dens_row<TWO, false>(S, t, l, NT, Pl, Ml, mu, mu_s, ox, sx, sy, G, pc, kray, kmie, nu_n1, ir_n1, acc);
       if (MX) {
         // Kahan sum over theta rows of the FP32 sums over one row
 #pragma unroll
         for (int j = 0; j < kDensMaxGroup; ++j) {
           if (j < G) {
-            Kahan3::add1(accs[6 * j], accs[6 * j + 3], acc[j].x);
-            Kahan3::add1(accs[6 * j + 1], accs[6 * j + 4], acc[j].y);
-            Kahan3::add1(accs[6 * j + 2], accs[6 * j + 5], acc[j].z);
+            Kahan3::add1(accs[(6 * j) * kDensThreads], accs[(6 * j + 3) * kDensThreads], acc[j].x);
+            Kahan3::add1(accs[(6 * j + 1) * kDensThreads], accs[(6 * j + 4) * kDensThreads], acc[j].y);
+            Kahan3::add1(accs[(6 * j + 2) * kDensThreads], accs[(6 * j + 5) * kDensThreads], acc[j].z);
             acc[j] = make_float3(0.f, 0.f, 0.f);
           }
         }
@@ -983,8 +1038,9 @@ __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned cha
         const size_t tt = ((size_t)zi * a.sc_mu + y) * a.W + x;
         float3 o = acc[j];
         if (MX)
-          o = make_float3(accs[6 * j] - accs[6 * j + 3], accs[6 * j + 1] - accs[6 * j + 4],
-                          accs[6 * j + 2] - accs[6 * j + 5]);
+          o = make_float3(accs[(6 * j) * kDensThreads] - accs[(6 * j + 3) * kDensThreads],
+                          accs[(6 * j + 1) * kDensThreads] - accs[(6 * j + 4) * kDensThreads],
+                          accs[(6 * j + 2) * kDensThreads] - accs[(6 * j + 5) * kDensThreads]);
         a.dens[tt] = store_round4(make_float4(o.x, o.y, o.z, 0.f), a.f16);
       }
     }
@@ -1141,12 +1197,14 @@ __device__ void tile_indirect(const DevAtmo& a, int order, int tile, unsigned ch
 }
 
 // V selects the occupancy variant chosen by the autotuner: V = 0 caps the
-// registers for 4 resident blocks per SM, V = 1 for 6.
-template <bool MX, int V> __global__ void __launch_bounds__(kDensThreads, V == 0 ? 4 : 6) k_density(LaunchArgs L) {
+// registers for 4 resident blocks per SM, V = 1 for 3. TWO: the launch of
+// order 2, whose lookups read the single-scattering Rayleigh and Mie tables.
+template <bool MX, int V, bool TWO>
+__global__ void __launch_bounds__(kDensThreads, V == 0 ? 4 : 3) k_density(LaunchArgs L) {
   extern __shared__ __align__(16) unsigned char smem[];
   int seg, job, tile;
   while (next_item(L, seg, job, tile)) {
-    if (seg == 0) tile_density<MX>(L.atm[job], L.order, tile, smem);
+    if (seg == 0) tile_density<MX, TWO>(L.atm[job], L.order, tile, smem);
     else tile_indirect<MX>(L.atm[job], L.order, tile, smem);
   }
 }
