@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <atomic>
 #include <cstdarg>
 #include <cstdio>
@@ -625,6 +626,16 @@ void fill_devatmo(DevAtmo& d, const fb_params& p, const fbi::Tuning& tun) {
   d.order = (int)p.order;
   d.f16 = p.storage == FB_STORAGE_F16;
   d.W = d.sc_nu * d.sc_mus;
+  {
+    const double R = d.bottom, T = d.top;
+    d.H2d = T * T - R * R;
+    d.Hd = std::sqrt(d.H2d);
+    d.Hf = (float)d.Hd;
+    d.inv_Hf = (float)(1.0 / d.Hd);
+    const double span = d.Hd - (T - R);
+    d.mus_inv_span = (float)(1.0 / span);
+    d.mus_inv_A = (float)(span / (-2.0 * (double)d.mu_s_min * R));
+  }
   const fbi::TuneEntry* te = fbi::tuning_find(tun, d.sc_r, d.sc_mu, d.sc_mus, d.sc_nu, (int)p.precision);
   d.dens_S = te ? te->dens_S : 0;
   d.dens_chunk = te ? te->dens_chunk : 0;

@@ -83,6 +83,13 @@ struct DevAtmo {
   int f16;         // round the scattering-class tables to half on store
   int W;           // sc_nu * sc_mus, width of the packed 3D scattering tables
   int dens_S, dens_chunk;  // scattering-density tile shape (0 = default; set by the autotuner)
+  // Per-atmosphere constants of the MIXED geometry, computed on the host in
+  // FP64 (correctly rounded, the values the device would compute) so that no
+  // thread repeats an FP64 square root or division per tile.
+  double H2d;                  // T^2 - R^2
+  double Hd;                   // sqrt(T^2 - R^2)
+  float Hf, inv_Hf;            // FP32 sqrt(T^2 - R^2) and its reciprocal
+  float mus_inv_span, mus_inv_A;  // mu_s mapping (scattering.h:48-56): 1 / (H - (T - R)), (H - (T - R)) / A'
   // outputs
   float4* tr;
   float4* ir;
@@ -343,8 +350,8 @@ struct Geo64 {
   __device__ __forceinline__ void init(const DevAtmo& a) {
     R = a.bottom;
     T = a.top;
-    H2 = T * T - R * R;
-    H = sqrt(H2);
+    H2 = a.H2d;  // T * T - R * R
+    H = a.Hd;    // sqrt(H2)
   }
   __device__ __forceinline__ double radius(double q) const { return sqrt(q + R * R); }
   // params.h:105-110 with the discriminant T^2 - r^2 (1 - mu^2) = (H^2 - q) + s^2.
@@ -446,10 +453,10 @@ struct GeoMx {
   __device__ __forceinline__ void init(const DevAtmo& a) {
     R = a.bottom;
     T = a.top;
-    H2 = (double)a.top * a.top - (double)a.bottom * a.bottom;
+    H2 = a.H2d;
     H2f = (float)H2;
-    H = (float)sqrt(H2);
-    inv_H = (float)(1.0 / sqrt(H2));
+    H = a.Hf;
+    inv_H = a.inv_Hf;
     trm1 = float(a.tr_mu - 1);
     trr1 = float(a.tr_r - 1);
     scr1 = float(a.sc_r - 1);
@@ -520,20 +527,18 @@ struct GeoMx {
 struct MuS32 {
   float R, H2, dmin, inv_span, inv_A, scale;
   __device__ __forceinline__ void init(const DevAtmo& a) {
-    const double Rd = a.bottom, Td = a.top;
-    const double H2d = Td * Td - Rd * Rd;
-    const double span = sqrt(H2d) - (Td - Rd);
     R = a.bottom;
-    H2 = (float)H2d;
-    dmin = (float)(Td - Rd);
-    inv_span = (float)(1.0 / span);
-    inv_A = (float)(span / (-2.0 * a.mu_s_min * Rd));
+    H2 = (float)a.H2d;
+    dmin = (float)((double)a.top - (double)a.bottom);
+    inv_span = a.mus_inv_span;
+    inv_A = a.mus_inv_A;
     scale = float(a.sc_mus - 1);
   }
   // texel coordinate within a nu slice
   __device__ __forceinline__ float texel(float mu_s) const {
     float s = R * mu_s;
-    float root = sqrtf(fmaf(s, s, H2));
+    const float disc = fmaf(s, s, H2);  // >= H^2 > 0
+    float root = disc * rsqrtf(disc);
     float d = s > 0.0f ? __fdividef(H2, s + root) : root - s;
     float aa = (d - dmin) * inv_span;
     return __fdividef(gmax(1.0f - aa * inv_A, 0.0f), 1.0f + aa) * scale;

@@ -96,12 +96,14 @@ __device__ __forceinline__ double warp_sum(double v) {
 // samples of the three optical lengths, then reduce with shuffles.
 template <bool MX> __device__ void tile_transmittance(const DevAtmo& a, int tile) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int t = tile * (kThreads / 32) + warp;
-  if (t >= a.tr_mu * a.tr_r) return;
-  const int i = t % a.tr_mu, j = t / a.tr_mu;
+  const int t0 = tile * (kThreads / 32);
+  const int t = t0 + warp;
+  const int ntr = a.tr_mu * a.tr_r;
   const int N = a.tr_steps;
   float sR, sM, sA;
   if (!MX) {
+    if (t >= ntr) return;
+    const int i = t % a.tr_mu, j = t / a.tr_mu;
     Geo32 G;
     G.init(a);
     float x_mu = float(i) / float(a.tr_mu - 1), x_r = float(j) / float(a.tr_r - 1);
@@ -128,18 +130,28 @@ template <bool MX> __device__ void tile_transmittance(const DevAtmo& a, int tile
     sM = warp_sum(sM);
     sA = warp_sum(sA);
   } else {
-    Geo64 G;
-    G.init(a);
-    double x_mu = double(i) / double(a.tr_mu - 1), x_r = double(j) / double(a.tr_r - 1);
-    double rho = G.H * x_r, q = rho * rho, r = G.radius(q);
-    double d_min = (G.H2 - q) / (G.T + r), d_max = rho + G.H;
-    double d = d_min + x_mu * (d_max - d_min);
-    double s = d == 0.0 ? r : gclamp((G.H2 - q - d * d) / (2.0 * d), -r, r);
-    const double dx = G.dist_top(q, s) / double(N);
-    // The march runs in FP32 on the FP64 ray state (q, 2 s, dx): r_k^2 - R^2 =
+    // The ray state of the CTA's texels (transmittance.comp:48-64 in FP64)
+    // is computed once per texel by one thread and shared: (q, 2 s, dx).
+    __shared__ float3 s_ray[kThreads / 32];
+    if (threadIdx.x < kThreads / 32 && t0 + (int)threadIdx.x < ntr) {
+      const int tt = t0 + threadIdx.x;
+      const int i = tt % a.tr_mu, j = tt / a.tr_mu;
+      Geo64 G;
+      G.init(a);
+      double x_mu = double(i) / double(a.tr_mu - 1), x_r = double(j) / double(a.tr_r - 1);
+      double rho = G.H * x_r, q = rho * rho, r = G.radius(q);
+      double d_min = (G.H2 - q) / (G.T + r), d_max = rho + G.H;
+      double d = d_min + x_mu * (d_max - d_min);
+      double s = d == 0.0 ? r : gclamp((G.H2 - q - d * d) / (2.0 * d), -r, r);
+      s_ray[threadIdx.x] = make_float3((float)q, (float)(2.0 * s), (float)(G.dist_top(q, s) / double(N)));
+    }
+    __syncthreads();
+    if (t >= ntr) return;
+    // The march runs in FP32 on the FP64 ray state: r_k^2 - R^2 =
     // q + d_k (2 s + d_k) keeps the altitude q_k / (r_k + R) free of the
     // cancellation of r_k - R, to ~1e-5 km where the ray grazes the ground.
-    const float qf = (float)q, two_sf = (float)(2.0 * s), dxf = (float)dx, Rf = a.bottom, R2f = Rf * Rf;
+    const float3 ray = s_ray[warp];
+    const float qf = ray.x, two_sf = ray.y, dxf = ray.z, Rf = a.bottom, R2f = Rf * Rf;
     float cR = 0.f, cM = 0.f, cA = 0.f;
     sR = sM = sA = 0.0f;
     for (int k = lane; k <= N; k += 32) {
@@ -154,11 +166,10 @@ template <bool MX> __device__ void tile_transmittance(const DevAtmo& a, int tile
       Kahan3::add1(sM, cM, profile_density(a.mie_d, h) * w);
       Kahan3::add1(sA, cA, profile_density(a.abs_d, h) * w);
     }
-    double dR = warp_sum((double)sR - (double)cR), dM = warp_sum((double)sM - (double)cM),
-           dA = warp_sum((double)sA - (double)cA);
-    sR = (float)(dR * dx);
-    sM = (float)(dM * dx);
-    sA = (float)(dA * dx);
+    // compensated lane sums, reduced in FP32 (32 terms)
+    sR = warp_sum(sR - cR) * dxf;
+    sM = warp_sum(sM - cM) * dxf;
+    sA = warp_sum(sA - cA) * dxf;
   }
   if (lane == 0) {
     float4 o;
@@ -1217,11 +1228,25 @@ __global__ void __launch_bounds__(kDensThreads, V == 0 ? 4 : 3) k_density(Launch
 // For each sample the CTA interpolates the density table in (mu, r) once into
 // a slab over x; each texel then blends four slab entries (two mu_s
 // neighbours in two nu slices).
+// Slab of one row: W entries plus one guard nu slice (sc_mus entries, zero)
+// read with weight 0 where nu = 1 selects the last slice.
+__host__ __device__ inline int ms_slab_row(int W, int sc_mus) { return W + sc_mus; }
 __host__ __device__ inline size_t ms_smem(int W, int steps, int sc_mus, int sc_nu) {
-  (void)sc_mus;
   (void)sc_nu;
   const int R = rows_per_tile(W);
-  return align16(sizeof(MSRec) * (size_t)R * (steps + 1)) + 2 * sizeof(float4) * (size_t)R * W;
+  return align16(sizeof(MSRec) * (size_t)R * (steps + 1)) + 2 * sizeof(float4) * (size_t)R * ms_slab_row(W, sc_mus);
+}
+
+// Position t in [0, n - 1] within a row of n texels as (i0, f): texel i0 in
+// [0, n - 1] and weight f of texel i0 + 1 (the value at t is p[i0] + f
+// (p[i0 + 1] - p[i0])); the clamp also maps NaN to 0. Rounding t - 1/2 to an
+// integer through the float adder gives floor(t), or floor(t) - 1 with f = 1
+// where t is an integer: the same interpolated value.
+__device__ __forceinline__ int row_pos(float t, float n_minus_1, float& f) {
+  t = fminf(fmaxf(t, 0.0f), n_minus_1);
+  const float y = (t - 0.5f) + kRoundMagic;
+  f = t - (y - kRoundMagic);
+  return max(__float_as_int(y) - kRoundMagicBits, 0);
 }
 
 template <bool MX, int TPT>
@@ -1234,8 +1259,13 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
   const int tid = threadIdx.x;
   MSRec* rec = (MSRec*)smem;
   float4* slab = (float4*)(smem + align16(sizeof(MSRec) * (size_t)R * NS));
+  const int SW = ms_slab_row(W, a.sc_mus);  // slab row stride (W + guard slice)
   const int slab_n = nrow * W;
-  const int slab_stride = R * W;
+  const int slab_stride = R * SW;
+  for (int k = tid; k < 2 * R * a.sc_mus; k += kThreads) {  // guard slices
+    const int b = k / (R * a.sc_mus), rem = k % (R * a.sc_mus);
+    slab[b * slab_stride + (rem / a.sc_mus) * SW + W + rem % a.sc_mus] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
   {  // this tile's sample records
     const int4* src = reinterpret_cast<const int4*>(a.g_ms + (size_t)row0 * NS);
     int4* dst = reinterpret_cast<int4*>(rec);
@@ -1243,8 +1273,8 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
     for (int k = tid; k < n16; k += kThreads) dst[k] = __ldg(src + k);
   }
   // per-texel constants (TPT texels per thread)
-  float c_rmus[TPT], c_nu[TPT], c_lerp[TPT], c_tex[TPT];
-  int c_lr[TPT], c_x[TPT];
+  float c_rmus[TPT], c_nu[TPT], c_lerp[TPT];
+  int c_lr[TPT], c_x[TPT], c_slice[TPT];
   Kahan3 acc[TPT];
   float3 part[TPT];
   MuS32 mus32;
@@ -1255,7 +1285,8 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
   for (int j = 0; j < TPT; ++j) {
     acc[j].init();
     part[j] = make_float3(0.f, 0.f, 0.f);
-    c_rmus[j] = c_nu[j] = c_lerp[j] = c_tex[j] = 0.f;
+    c_rmus[j] = c_nu[j] = c_lerp[j] = 0.f;
+    c_slice[j] = 0;
     const int k = tid + j * kThreads;
     c_lr[j] = k / W;
     c_x[j] = k - c_lr[j] * W;
@@ -1266,9 +1297,9 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
       c_rmus[j] = rmus;
       // scattering.h:146-148
       const float tcx = (nu + 1.0f) / 2.0f * float(a.sc_nu - 1);
-      const float fl = floorf(tcx);
+      const float fl = fminf(fmaxf(floorf(tcx), 0.0f), float(a.sc_nu - 1));
       c_lerp[j] = tcx - fl;
-      c_tex[j] = fl;
+      c_slice[j] = (int)fl * a.sc_mus;
     }
   }
   __syncthreads();
@@ -1305,7 +1336,7 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
         v.y = fmaf(w11, a11.y, fmaf(w01, a01.y, fmaf(w10, a10.y, w00 * a00.y)));
         v.z = fmaf(w11, a11.z, fmaf(w01, a01.z, fmaf(w10, a10.z, w00 * a00.z)));
         v.w = 0.f;
-        dst[k] = v;
+        dst[c_lr[j] * SW + c_x[j]] = v;
       }
     }
   };
@@ -1320,27 +1351,25 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
       if (tid + j * kThreads < slab_n) {
         const MSRec& o = rec[c_lr[j] * NS + i];
         const float nu = c_nu[j];
-        const float tx = c_tex[j];
-        Axis x0, x1;
+        // position within a nu slice, texel units (scattering.h:48-56, 149-151):
+        // both slices of the lookup share it
+        float t;
         if (!MX) {
-          // sampler coordinate ((tex_x + u_mu_s) / nu_size) W - 1/2 (scattering.h:149-151)
           const float mu_s_i = clamp_cosine((c_rmus[j] + o.d * nu) * o.inv_r);
-          const float t = fmaf(tx + musref.coord(mu_s_i), fmus, -0.5f);
-          x0 = axis_texel(t, W);
-          x1 = axis_texel(t + fmus, W);
+          t = fmaf(musref.coord(mu_s_i), fmus, -0.5f);
         } else {
-          // texel coordinate of slice k: k * mu_s_size + y (mu_s_size - 1)
           const float mu_s_i = clamp_cosine(fmaf(o.d, nu, c_rmus[j]) * o.inv_r);
-          const float t = mus32.texel(mu_s_i);
-          x0 = axis_texel(fmaf(tx, fmus, t), W);
-          x1 = axis_texel(fmaf(tx + 1.0f, fmus, t), W);
+          t = mus32.texel(mu_s_i);
         }
-        const float4* sl = cur + c_lr[j] * W;
-        const float4 p00 = sl[x0.i0], p01 = sl[x0.i1], p10 = sl[x1.i0], p11 = sl[x1.i1];
+        float fx;
+        const int i0 = row_pos(t, fmus - 1.0f, fx);
+        // slices k and k + 1 of the row (k + 1 = nu_size: the zero guard slice)
+        const float4* sl = cur + c_lr[j] * SW + c_slice[j] + i0;
+        const float4 p00 = sl[0], p01 = sl[1], p10 = sl[a.sc_mus], p11 = sl[a.sc_mus + 1];
         const float lf = c_lerp[j];
-        const float ax = fmaf(p01.x - p00.x, x0.f, p00.x), bx = fmaf(p11.x - p10.x, x1.f, p10.x);
-        const float ay = fmaf(p01.y - p00.y, x0.f, p00.y), by = fmaf(p11.y - p10.y, x1.f, p10.y);
-        const float az = fmaf(p01.z - p00.z, x0.f, p00.z), bz = fmaf(p11.z - p10.z, x1.f, p10.z);
+        const float ax = fmaf(p01.x - p00.x, fx, p00.x), bx = fmaf(p11.x - p10.x, fx, p10.x);
+        const float ay = fmaf(p01.y - p00.y, fx, p00.y), by = fmaf(p11.y - p10.y, fx, p10.y);
+        const float az = fmaf(p01.z - p00.z, fx, p00.z), bz = fmaf(p11.z - p10.z, fx, p10.z);
         const float3 J = make_float3(fmaf(bx - ax, lf, ax), fmaf(by - ay, lf, ay), fmaf(bz - az, lf, az));
         const float3 v = J * make_float3(o.tvwx, o.tvwy, o.tvwz);
         if (!MX) {
