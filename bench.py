@@ -137,13 +137,15 @@ def max_over_ranks(world, v):
 
 
 # ------------------------------------------------------------- roofline ---
-# Algorithmic FLOPs: the shader arithmetic of the reference's algorithm per
-# output texel, op-counted on the oracle's restatement over the first 16
-# atmospheres of this workload (`python oracle/count_flops.py`; adds, muls,
-# divs, sqrts and transcendentals one FLOP each, sampler filtering and
-# literal-only expressions not counted). The dominant launch computes the
-# scattering density of order n (2 * 16^2 directions per texel, 162.6 FLOPs
-# per direction at n >= 3) and the indirect irradiance of order n - 1.
+# The roofline of the dominant launch (scattering density of order n >= 3 plus
+# the indirect irradiance of order n - 1) is reported on the FP32 pipe: the
+# FLOPs the kernel executes per direction evaluation (measured with ncu on the
+# same launch, a committed profile summary) times the directions of the
+# launch, over its CUDA-event time. Beside it: the reference's quadrature
+# arithmetic per output texel, op-counted on the oracle's restatement over the
+# first 16 atmospheres of this workload (`python oracle/count_flops.py`; adds,
+# muls, divs, sqrts and transcendentals one FLOP each, sampler filtering and
+# literal-only expressions not counted; 162.6 FLOPs per direction at n >= 3).
 FLOP_PER_TEXEL = {
     "transmittance": 28311.7,
     "direct_irradiance": 34.0,
@@ -155,19 +157,22 @@ FLOP_PER_TEXEL = {
     "multiple_scattering": 8332.2,
 }
 FLOP_PER_ATMOSPHERE = 350185724984.0  # default sizes, 4 orders (same count)
+# committed ncu summaries the roofline figures come from
+DENSITY_PROFILE = "density_multiple_uniform16_mixed_ncu.md"
+LAUNCH_PROFILE = "launches_uniform256_mixed.md"
 
 
 def fp32_peak_tflops(sms, mhz):
     return sms * 128 * 2 * mhz * 1e6 / 1e12
 
 
-def read_traffic():
-    path = os.path.join(ROOT, "profiles", "density_default_mixed_ncu.txt")
+def profile_value(name, key):
+    """A `key: value` line of a committed ncu summary under profiles/."""
     try:
-        for line in open(path):
-            if line.startswith("dram_bytes_per_launch_order3:"):
+        for line in open(os.path.join(ROOT, "profiles", name)):
+            if line.startswith(key + ":"):
                 return float(line.split(":", 1)[1])
-    except OSError:
+    except (OSError, ValueError):
         pass
     return None
 
@@ -307,11 +312,17 @@ def run_ours(a):
     dens = [r for launches in prof for r in launches if r["kernel"] == "density+indirect" and r["order"] >= 3]
     dens_ms = sum(r["ms"] for r in dens) / max(len(dens), 1)
     sms = builder.sm_count
-    flops = a.batch * (sizes[2] * FLOP_PER_TEXEL["density_order3"] + sizes[1] * FLOP_PER_TEXEL["indirect_order2"])
-    achieved = flops / (dens_ms / 1e3) / 1e12
+    # executed FP32 FLOPs per direction evaluation of this launch (ncu) and
+    # the reference's quadrature FLOPs per texel (oracle op count)
+    directions = a.batch * sizes[2] * 2 * params[0].density_samples ** 2
+    exec_per_dir = profile_value(DENSITY_PROFILE, "fp32_flop_per_direction_order3")
+    ref_flops = a.batch * (sizes[2] * FLOP_PER_TEXEL["density_order3"] + sizes[1] * FLOP_PER_TEXEL["indirect_order2"])
     mhz = (clk or {}).get("sm_mhz") or 2070.0
     peak = fp32_peak_tflops(sms, mhz)
-    traffic = read_traffic()
+    exec_flops = directions * exec_per_dir if exec_per_dir else None
+    achieved = exec_flops / (dens_ms / 1e3) / 1e12 if exec_flops else None
+    ref_achieved = ref_flops / (dens_ms / 1e3) / 1e12
+    traffic = profile_value(LAUNCH_PROFILE, "dram_bytes_per_launch_order3")
     peaks = measured_peaks()
 
     out = {
@@ -338,15 +349,23 @@ def run_ours(a):
                 "d2h_bytes_per_step": a.batch * per_atm},
         "gpu_launches": sum(len(x) for x in prof),
         "roofline": {"bound": "fp32", "kernel": "k_density (scattering density + indirect irradiance), order >= 3",
-                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak if achieved else None,
                      "peak_source": "152 SMs x 128 FP32 lanes x 2 FLOP x median SM clock under load (%d MHz); "
-                                    "the kernel uses neither HBM bandwidth nor tensor cores at their limits" % mhz,
-                     "launch_ms": dens_ms, "flop_per_launch": flops,
-                     "flop_source": "reference shader arithmetic per texel, op-counted on the oracle "
-                                    "(oracle/count_flops.py)",
-                     "hbm": {"achieved_gbs": (traffic or 0) / (dens_ms / 1e3) / 1e9 if traffic else None,
+                                    "no tensor-core work, HBM far from its limit" % mhz,
+                     "launch_ms": dens_ms, "flop_per_unit": exec_per_dir, "units_per_launch": directions,
+                     "unit_name": "direction evaluations (texels x 512 sphere directions)",
+                     "flop_source": "executed FP32 FLOPs (FADD + FMUL + 2 FFMA) per direction, ncu, profiles/"
+                                    + DENSITY_PROFILE,
+                     "traffic": traffic, "traffic_source": "ncu DRAM bytes of the same launch, profiles/" + LAUNCH_PROFILE,
+                     "hbm": {"achieved_gbs": traffic / (dens_ms / 1e3) / 1e9 if traffic else None,
                              "peak_gbs": peaks.get("hbm_gbs"), "peak_source": "MEASURED_PEAKS.json"},
-                     "traffic": traffic},
+                     "reference_algorithm": {
+                         "achieved": ref_achieved, "frac": ref_achieved / peak,
+                         "flop_per_texel": FLOP_PER_TEXEL["density_order3"],
+                         "note": "the reference's quadrature arithmetic (oracle op count, oracle/count_flops.py) "
+                                 "delivered per second: the kernel executes fewer FLOPs per direction than the "
+                                 "reference's shader code (per-tile reduced tables replace the 4D lookups)"}},
         "kernels_ms": {k: sum(r["ms"] for r in v) / len(v) for k, v in sorted(kernels.items())},
         "latency_ms": {"p50": statistics.median(step_ms), "p99": float(np.quantile(step_ms, 0.99))},
         "graph": {"ms_per_step": graph_ms, "value": world * a.batch / (graph_ms / 1e3)},
