@@ -52,6 +52,13 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "plain"],
                     help="arithmetic of the batch (the headline is mixed)")
+    ap.add_argument("--workload", default="uniform", choices=["uniform", "uneven", "serve"],
+                    help="uniform: the headline batch; uneven: 96 atmospheres over three table classes, "
+                         "orders 2-8; serve: open-loop Poisson requests through the request loop")
+    ap.add_argument("--rates", default="50,200,1000", help="serve: offered request rates (req/s)")
+    ap.add_argument("--duration", type=float, default=60.0, help="serve: seconds of arrivals per rate")
+    ap.add_argument("--max-queue", type=int, default=512,
+                    help="serve: queued requests beyond which new ones are refused (load shedding)")
     return ap.parse_args()
 
 
@@ -426,10 +433,238 @@ def run_reference(a):
     print(json.dumps(out))
 
 
+# ----------------------------------------------------------- uneven batch ---
+def run_uneven(a):
+    """96 atmospheres (seed 1) split evenly over the default, half and double
+    table classes, orders uniform in 2-8, one batch build per step (one
+    persistent launch per pass group, replayed from a CUDA graph)."""
+    world, rank, local = dist()
+    import numpy as np
+    import torch
+    torch.cuda.set_device(local)
+    from fuzzyblue_gb300 import workloads
+    from fuzzyblue_gb300.api import Builder, build_batch
+    from fuzzyblue_gb300.params import PRECISION_MIXED, PRECISION_PLAIN
+    from fuzzyblue_gb300 import _native as N
+    builder = Builder(local)
+    stream = torch.cuda.Stream()
+    prec = PRECISION_MIXED if a.precision == "mixed" else PRECISION_PLAIN
+    params = workloads.uneven_batch(96, seed=1, precision=prec)
+    classes, seen = [], set()
+    for p in params:
+        key = p.scattering_extent()
+        if key not in seen:
+            seen.add(key)
+            classes.append(p)
+    if not a.no_autotune:
+        builder.autotune(classes, batch=4)
+    tuned = [builder.tuned_shape(c) for c in classes]
+    for _ in range(a.warmup):
+        q = build_batch(builder, params, stream=stream)
+        q.wait()
+        q.release()
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(a.steps):
+        q = build_batch(builder, params, stream=stream)
+        q.wait()
+        q.release()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / a.steps
+    # end to end: every table of every atmosphere into pinned host memory
+    bufs = {}
+    for p in params:
+        n = 4 * sum(p.texel_counts())
+        key = p.scattering_extent()
+        if key not in bufs:
+            bufs[key] = torch.empty(n, dtype=torch.float32, pin_memory=True).numpy()
+    d2h = 0
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        q = build_batch(builder, params, stream=stream)
+        q.wait()
+        for i, p in enumerate(params):
+            ntr, nir, nsc = p.texel_counts()
+            base = bufs[p.scattering_extent()].ctypes.data
+            N.check(N.lib().fb_atmosphere_copy_to_host(q.atmosphere(i)._h, stream.cuda_stream, base,
+                                                       base + 16 * ntr, base + 16 * (ntr + nir)), "copy_to_host")
+            d2h += 16 * (ntr + nir + nsc)
+        q.release()
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / a.steps
+    per_class = {}
+    for p in params:
+        c = "x".join(str(v) for v in p.scattering_extent())
+        per_class[c] = per_class.get(c, 0) + 1
+    out = {
+        "metric": "atmospheres/s, uneven batch of 96 over three table classes, orders 2-8, %s precision"
+                  % a.precision,
+        "value": 96 / (ms / 1e3), "unit": "atmospheres/s", "n_gpus": 1, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 with f64 ray geometry and order accumulation" if a.precision == "mixed" else "f32",
+        "data": "synthetic: seeded atmospheres (fuzzyblue_gb300.workloads.uneven_batch, seed 1)",
+        "config": {"workload": "uneven batch: 96 seeded atmospheres (seed 1), default / half / double table "
+                               "classes 32 each, orders uniform in 2-8", "classes": per_class,
+                   "orders": sorted(set(p.order for p in params)), "precision": a.precision,
+                   "l2": "inputs larger than L2"},
+        "clocks": clk,
+        "e2e": {"value": 96 / e2e_s, "unit": "atmospheres/s", "h2d_bytes_per_step": 96 * 384,
+                "d2h_bytes_per_step": d2h // a.steps},
+        "tile_shapes": tuned,
+    }
+    print(json.dumps(out))
+    builder.close()
+
+
+# ---------------------------------------------------------------- serving ---
+def run_serve(a):
+    """Open-loop Poisson request stream (seed 2) through the request loop
+    (fb_server_*): each request one atmosphere drawn from the uniform-batch
+    distributions, table class 60/30/10 default / half / double, orders 2-8,
+    admitted under a 120 GB HBM budget, finished tables resident (LRU). The
+    plain one-at-a-time path is measured as per-request build times of plain
+    FP32 single builds per (class, order), replayed in arrival order through
+    one FIFO server with the same queue limit."""
+    import threading
+    import numpy as np
+    import torch
+    torch.cuda.set_device(0)
+    from fuzzyblue_gb300 import workloads
+    from fuzzyblue_gb300 import _native as N
+    from fuzzyblue_gb300.api import Atmosphere, Builder, Server
+    from fuzzyblue_gb300.params import PRECISION_MIXED, PRECISION_PLAIN
+    builder = Builder(0)
+    names = ("default", "half", "double")
+    probe = workloads.draw_atmosphere(np.random.default_rng(99), precision=PRECISION_MIXED)
+    if not a.no_autotune:
+        builder.autotune([probe.replace(**workloads.CLASSES[c]) for c in names], batch=4)
+
+    def cls_of(p):
+        for c in ("double", "half"):  # the default class has no overrides: test it last
+            if all(getattr(p, k) == v for k, v in workloads.CLASSES[c].items()):
+                return c
+        return "default"
+
+    # plain one-at-a-time service times per (class, order), FP32
+    service = {}
+    for c in names:
+        for order in range(2, 9):
+            q0 = probe.replace(precision=PRECISION_PLAIN, order=order, **workloads.CLASSES[c])
+            ts = []
+            for rep in range(3):
+                t0 = time.perf_counter()
+                q = Atmosphere.build(builder, q0)
+                q.wait()
+                ts.append(time.perf_counter() - t0)
+                q.release()
+            service[(c, order)] = min(ts[1:])
+    lines = []
+    for rate in [float(x) for x in a.rates.split(",")]:
+        rng = np.random.default_rng(2)
+        arrivals, t = [], 0.0
+        while True:
+            t += float(rng.exponential(1.0 / rate))
+            if t > a.duration:
+                break
+            arrivals.append(t)
+        reqs = [workloads.serving_request(rng) for _ in arrivals]
+        srv = Server(builder, hbm_budget_bytes=120 * 10 ** 9, max_queue=a.max_queue)
+        submit_at, done_at, rejected, fresh = {}, {}, [0], []
+        lock = threading.Lock()
+        start = time.perf_counter() + 0.05
+
+        def submitter():
+            for at, p in zip(arrivals, reqs):
+                delay = start + at - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+                try:
+                    tk = srv.submit(p)
+                except N.FuzzyblueError:
+                    with lock:
+                        rejected[0] += 1
+                    continue
+                with lock:
+                    submit_at[tk] = start + at
+                    fresh.append(tk)
+        th = threading.Thread(target=submitter)
+        th.start()
+        outstanding = []
+        deadline = start + a.duration + 120.0
+        while time.perf_counter() < deadline:
+            with lock:
+                outstanding.extend(fresh)
+                fresh.clear()
+            still = []
+            for tk in outstanding:
+                if srv.poll(tk) is not None:
+                    done_at[tk] = time.perf_counter()
+                    srv.release(tk)
+                else:
+                    still.append(tk)
+            outstanding = still
+            if not th.is_alive() and not outstanding:
+                with lock:
+                    if not fresh:
+                        break
+            time.sleep(0.0005)
+        th.join()
+        st = srv.stats()
+        srv.close()
+        lat = np.array([done_at[k] - submit_at[k] for k in done_at]) * 1e3
+        end = max(done_at.values()) if done_at else start
+        served = {"completed": len(done_at), "rejected": rejected[0],
+                  "throughput": len(done_at) / max(end - start, 1e-9),
+                  "p50_ms": float(np.percentile(lat, 50)) if len(lat) else None,
+                  "p99_ms": float(np.percentile(lat, 99)) if len(lat) else None,
+                  "server_p50_ms": st["p50_ms"], "server_p99_ms": st["p99_ms"], "batches": st["batches"],
+                  "mean_batch": st["mean_batch"], "evictions": st["evictions"]}
+        # the plain path on the same arrivals: one FIFO server, same queue limit
+        free_at, lat_p, comp, rej_p, queue = 0.0, [], 0, 0, []
+        for at, p in zip(arrivals, reqs):
+            queue = [x for x in queue if x > at]  # completion times still ahead
+            if len(queue) > a.max_queue:
+                rej_p += 1
+                continue
+            s_t = service[(cls_of(p), p.order)]
+            begin = max(at, free_at)
+            free_at = begin + s_t
+            queue.append(free_at)
+            lat_p.append((free_at - at) * 1e3)
+            comp += 1
+        plain = {"completed": comp, "rejected": rej_p, "throughput": comp / max(free_at, 1e-9),
+                 "p50_ms": float(np.percentile(lat_p, 50)), "p99_ms": float(np.percentile(lat_p, 99))}
+        lines.append({"offered_rate": rate, "requests": len(arrivals), "served": served, "plain": plain,
+                      "served_over_plain_throughput": served["throughput"] / plain["throughput"]})
+    out = {
+        "metric": "served atmospheres/s and p50/p99 request latency, Poisson open loop",
+        "value": max(l["served"]["throughput"] for l in lines), "unit": "atmospheres/s", "n_gpus": 1,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 with f64 ray geometry and order accumulation",
+        "data": "synthetic: seeded requests (fuzzyblue_gb300.workloads.serving_request, seed 2)",
+        "config": {"workload": "serving: open-loop Poisson requests, class 60/30/10 default / half / double, "
+                               "orders 2-8, 120 GB HBM budget, LRU-resident tables",
+                   "duration_s": a.duration, "max_queue": a.max_queue,
+                   "plain_path": "plain FP32 single builds per (class, order), measured, replayed FIFO"},
+        "rates": lines,
+    }
+    print(json.dumps(out))
+    builder.close()
+
+
 def main():
     a = parse()
     if a.impl == "reference":
         run_reference(a)
+    elif a.workload == "uneven":
+        run_uneven(a)
+    elif a.workload == "serve":
+        run_serve(a)
     else:
         run_ours(a)
 

@@ -660,7 +660,8 @@ void pending_destroy(fb_pending* p) {
 
 // Plans and enqueues a build of `count` atmospheres on `s`. With use_graph the
 // launch sequence is captured into a CUDA graph and replayed.
-int build(fb_builder* b, cudaStream_t s, const fb_params* params, uint32_t count, bool use_graph, fb_pending** out) {
+int build(fb_builder* b, cudaStream_t s, const fb_params* params, uint32_t count, bool use_graph, fb_pending** out,
+          int max_items_per_cta) {
   if (!b || !params || !out || count == 0) return fail(FB_ERR_INVALID_ARGUMENT, "invalid arguments");
   *out = nullptr;
   for (uint32_t i = 0; i < count; ++i) {
@@ -774,7 +775,9 @@ int build(fb_builder* b, cudaStream_t s, const fb_params* params, uint32_t count
     R.block = L.pass == fb::kPassDensity ? fb::kDensThreads : fb::kThreads;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, R.fn, R.block, R.smem) != cudaSuccess || per_sm < 1)
       return bail(FB_ERR_CUDA, "occupancy query failed");
-    R.grid = std::max(1, std::min(total, per_sm * b->sms));
+    R.args.max_items = std::max(0, max_items_per_cta);
+    R.grid = max_items_per_cta > 0 ? std::max(1, (total + max_items_per_cta - 1) / max_items_per_cta)
+                                   : std::max(1, std::min(total, per_sm * b->sms));
     std::memset(&R.info, 0, sizeof(R.info));
     R.info.kernel = (uint32_t)L.pass;
     R.info.order = (uint32_t)L.order;

@@ -49,7 +49,11 @@ const fb_params& atmosphere_params(const fb_atmosphere* a);
 void atmosphere_set_stream(fb_atmosphere* a, cudaStream_t s);
 void atmosphere_tables(const fb_atmosphere* a, float4** tr, float4** ir, float4** sc);
 
-int build(fb_builder* b, cudaStream_t s, const fb_params* params, uint32_t count, bool use_graph, fb_pending** out);
+// max_items_per_cta > 0: every CTA exits after that many work items and the
+// grid covers the launch's items (the request loop uses it so that CTAs of
+// concurrent batches on other streams interleave); 0: persistent grids.
+int build(fb_builder* b, cudaStream_t s, const fb_params* params, uint32_t count, bool use_graph, fb_pending** out,
+          int max_items_per_cta = 0);
 void pending_destroy(fb_pending* p);
 // Removes atmosphere `index` from the pending handle (ownership to the caller).
 fb_atmosphere* pending_detach(fb_pending* p, uint32_t index);

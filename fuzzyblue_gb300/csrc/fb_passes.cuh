@@ -42,10 +42,18 @@ struct LaunchArgs {
   int nseg;
   int order;  // k_density / k_multiple: order n computed (indirect irradiance integrates n-1)
   unsigned int* counter;
+  // Items a CTA takes before it exits (0: no limit, the CTA runs until the
+  // work list is empty). A limit lets the block scheduler interleave CTAs of
+  // other streams (by priority) between items; the grid then covers the work.
+  int max_items;
 };
 
-__device__ __forceinline__ bool next_item(const LaunchArgs& L, int& seg, int& job, int& tile) {
+// Takes the next work item of the launch for this CTA; `taken` counts the
+// items this CTA has taken (for LaunchArgs::max_items).
+__device__ __forceinline__ bool next_item(const LaunchArgs& L, int& seg, int& job, int& tile, int& taken) {
   __shared__ int s_item;
+  if (L.max_items > 0 && taken >= L.max_items) return false;
+  ++taken;
   __syncthreads();
   if (threadIdx.x == 0) s_item = (int)atomicAdd(L.counter, 1u);
   __syncthreads();
@@ -293,7 +301,8 @@ __host__ __device__ inline int tiles_geometry(int W, int sc_mu, int sc_r) {
 
 template <bool MX> __global__ void __launch_bounds__(kThreads) k_transmittance(LaunchArgs L) {
   int seg, job, tile;
-  while (next_item(L, seg, job, tile)) {
+  int taken = 0;
+  while (next_item(L, seg, job, tile, taken)) {
     if (seg == 0) tile_transmittance<MX>(L.atm[job], tile);
     else tile_geometry<MX>(L.atm[job], tile);
   }
@@ -640,7 +649,8 @@ __device__ void tile_single(const DevAtmo& a, int tile, unsigned char* smem) {
 template <bool MX> __global__ void __launch_bounds__(kThreads) k_single(LaunchArgs L) {
   extern __shared__ __align__(16) unsigned char smem[];
   int seg, job, tile;
-  while (next_item(L, seg, job, tile)) {
+  int taken = 0;
+  while (next_item(L, seg, job, tile, taken)) {
     if (seg == 0) tile_single<MX>(L.atm[job], tile, smem);
     else if (seg == 1) tile_direct<MX>(L.atm[job], tile);
     else if (seg == 2) tile_msrec<MX>(L.atm[job], tile);
@@ -1214,7 +1224,8 @@ template <bool MX, int V, bool TWO>
 __global__ void __launch_bounds__(kDensThreads, V == 0 ? 4 : 3) k_density(LaunchArgs L) {
   extern __shared__ __align__(16) unsigned char smem[];
   int seg, job, tile;
-  while (next_item(L, seg, job, tile)) {
+  int taken = 0;
+  while (next_item(L, seg, job, tile, taken)) {
     if (seg == 0) tile_density<MX, TWO>(L.atm[job], L.order, tile, smem);
     else tile_indirect<MX>(L.atm[job], L.order, tile, smem);
   }
@@ -1427,7 +1438,8 @@ template <bool MX, int TPT, int V>
 __global__ void __launch_bounds__(kThreads, TPT <= 2 ? (V == 0 ? 4 : 3) : (V == 0 ? 2 : 1)) k_multiple(LaunchArgs L) {
   extern __shared__ __align__(16) unsigned char smem[];
   int seg, job, tile;
-  while (next_item(L, seg, job, tile)) tile_multiple<MX, TPT>(L.atm[job], L.order, tile, smem);
+  int taken = 0;
+  while (next_item(L, seg, job, tile, taken)) tile_multiple<MX, TPT>(L.atm[job], L.order, tile, smem);
 }
 
 // ------------------------------------------------------ tile geometry ----

@@ -6,9 +6,12 @@
 // One scheduler thread owns every CUDA call of the server. Each pass of its
 // loop (1) collects finished batches (a host callback after each batch wakes
 // it), moving their tables into the resident cache and freeing their
-// temporaries; (2) admits queued requests in arrival order while the budget
-// allows (evicting unpinned resident tables, least recently used first) and a
-// stream is free, launching them as one batch build; (3) sleeps until woken.
+// temporaries; (2) while a stream is free, takes the oldest queued request
+// and every queued request of its table class, in arrival order, while the
+// budget allows (evicting unpinned resident tables, least recently used
+// first), and launches them as one batch build - cheap batches on
+// high-priority streams, with CTAs that exit after a few work items so that
+// they interleave with a long build already running; (3) sleeps until woken.
 // Requests for parameters already resident or in flight share that result.
 #include <cuda_runtime.h>
 
@@ -28,6 +31,9 @@
 #include "fb_internal.h"
 
 namespace {
+
+// Work items a CTA of a served build takes before it exits.
+constexpr int kServeItemsPerCta = 2;
 
 double now_ms() {
   using namespace std::chrono;
@@ -93,6 +99,7 @@ struct fb_server {
   std::vector<Batch*> inflight;
   std::vector<cudaStream_t> streams;
   std::vector<bool> stream_busy;
+  std::vector<bool> stream_high;  // high-priority stream (cheap batches)
   size_t resident_bytes = 0, inflight_bytes = 0;
   uint64_t next_ticket = 1, clock = 0;
   fb_server_stats st;
@@ -189,31 +196,81 @@ void collect(fb_server* s) {
   evict(s, 0, true);
 }
 
-void admit(fb_server* s) {
+// Work of one request in texel-orders (scattering texels x orders): the
+// scheduler's cost estimate.
+double cost_of(const fb_params& p) {
+  const fb_params_raw& r = p.raw;
+  return (double)r.scattering_r_size * r.scattering_mu_size * r.scattering_mu_s_size * r.scattering_nu_size *
+         std::max(1u, p.order);
+}
+// Requests that share a batch: the same table class (scattering sizes) and
+// precision, so that a cheap request never waits for an expensive one.
+bool same_class(const fb_params& a, const fb_params& b) {
+  return a.raw.scattering_r_size == b.raw.scattering_r_size && a.raw.scattering_mu_size == b.raw.scattering_mu_size &&
+         a.raw.scattering_mu_s_size == b.raw.scattering_mu_s_size &&
+         a.raw.scattering_nu_size == b.raw.scattering_nu_size && a.precision == b.precision;
+}
+// Batches up to this cost (texel-orders) run on the high-priority streams.
+constexpr double kCheapBatch = 1048576.0 * 8;
+
+// Drops queue entries that no longer wait (cancelled, or shared with a
+// resident / in-flight result) from the front.
+bool settle_head(fb_server* s) {
   while (!s->queue.empty()) {
+    const uint64_t t = s->queue.front();
+    auto it = s->reqs.find(t);
+    if (it == s->reqs.end() || it->second.state != State::Queued) {
+      s->queue.pop_front();
+      continue;
+    }
+    Request& r = it->second;
+    auto ex = s->entries.find(r.key);
+    if (ex == s->entries.end()) return true;
+    s->st.cache_hits++;
+    s->queue.pop_front();
+    if (ex->second->ready) complete_request(s, t, ex->second);
+    else {
+      r.state = State::Running;
+      ex->second->waiters.push_back(t);
+    }
+  }
+  return false;
+}
+
+void admit(fb_server* s) {
+  while (settle_head(s)) {
+    const fb_params head = s->reqs[s->queue.front()].params;
+    // the head request's class, then every queued request of that class in
+    // arrival order (shared results are settled as they are met)
+    const bool cheap = cost_of(head) <= kCheapBatch;
     int slot = -1;
-    for (size_t k = 0; k < s->streams.size(); ++k)
-      if (!s->stream_busy[k]) {
-        slot = (int)k;
-        break;
-      }
+    for (int pass = 0; pass < 2 && slot < 0; ++pass)
+      for (size_t k = 0; k < s->streams.size(); ++k)
+        if (!s->stream_busy[k] && (pass == 1 || s->stream_high[k] == cheap)) {
+          slot = (int)k;
+          break;
+        }
     if (slot < 0) return;
     Batch* bt = new Batch();
     std::vector<fb_params> params;
-    std::vector<uint64_t> taken;
     size_t bytes = 0;
-    while (!s->queue.empty() && params.size() < s->cfg.max_batch) {
-      const uint64_t t = s->queue.front();
+    bool full = false;
+    for (auto qi = s->queue.begin(); qi != s->queue.end() && params.size() < s->cfg.max_batch && !full;) {
+      const uint64_t t = *qi;
       auto it = s->reqs.find(t);
       if (it == s->reqs.end() || it->second.state != State::Queued) {
-        s->queue.pop_front();
+        qi = s->queue.erase(qi);
         continue;
       }
       Request& r = it->second;
+      if (!same_class(r.params, head)) {
+        ++qi;
+        continue;
+      }
       auto ex = s->entries.find(r.key);
       if (ex != s->entries.end()) {  // resident or in flight: share it
         s->st.cache_hits++;
-        s->queue.pop_front();
+        qi = s->queue.erase(qi);
         if (ex->second->ready) complete_request(s, t, ex->second);
         else {
           r.state = State::Running;
@@ -223,7 +280,10 @@ void admit(fb_server* s) {
       }
       if (s->resident_bytes + s->inflight_bytes + bytes + r.need > s->cfg.hbm_budget_bytes) {
         evict(s, bytes + r.need, false);
-        if (s->resident_bytes + s->inflight_bytes + bytes + r.need > s->cfg.hbm_budget_bytes) break;
+        if (s->resident_bytes + s->inflight_bytes + bytes + r.need > s->cfg.hbm_budget_bytes) {
+          full = true;
+          break;
+        }
       }
       Entry* e = new Entry();
       e->key = r.key;
@@ -232,16 +292,16 @@ void admit(fb_server* s) {
       s->entries[r.key] = e;
       bt->entries.push_back(e);
       params.push_back(r.params);
-      taken.push_back(t);
       bytes += r.need;
       r.state = State::Running;
-      s->queue.pop_front();
+      qi = s->queue.erase(qi);
     }
     if (params.empty()) {
       delete bt;
       return;
     }
-    int rc = fbi::build(s->b, s->streams[slot], params.data(), (uint32_t)params.size(), true, &bt->pending);
+    int rc = fbi::build(s->b, s->streams[slot], params.data(), (uint32_t)params.size(), true, &bt->pending,
+                        kServeItemsPerCta);
     if (rc != FB_OK) {
       for (size_t k = 0; k < bt->entries.size(); ++k) {
         Entry* e = bt->entries[k];
@@ -307,15 +367,27 @@ extern "C" int fb_server_create(fb_builder* b, const fb_server_config* cfg, fb_s
     delete s;
     return fail_srv(FB_ERR_CUDA, "cudaSetDevice failed");
   }
+  // Half the streams (at least one) at the device's highest priority for
+  // cheap batches, the rest at the lowest: with CTAs that exit after a few
+  // work items, the block scheduler serves a cheap request's kernels ahead of
+  // an expensive build already running.
+  int prio_low = 0, prio_high = 0;
+  if (cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high) != cudaSuccess) {
+    cudaGetLastError();
+    prio_low = prio_high = 0;
+  }
+  const uint32_t n_high = std::max(1u, s->cfg.max_inflight / 2);
   for (uint32_t k = 0; k < s->cfg.max_inflight; ++k) {
     cudaStream_t st;
-    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+    const bool high = k < n_high;
+    if (cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, high ? prio_high : prio_low) != cudaSuccess) {
       for (cudaStream_t x : s->streams) cudaStreamDestroy(x);
       delete s;
       return fail_srv(FB_ERR_CUDA, "cudaStreamCreate failed");
     }
     s->streams.push_back(st);
     s->stream_busy.push_back(false);
+    s->stream_high.push_back(high);
   }
   s->b = b;
   fbi::builder_ref(b);
