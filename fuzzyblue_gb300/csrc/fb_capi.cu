@@ -288,9 +288,9 @@ extern "C" int fb_builder_create(int device, fb_builder** out) {
   }
   for (int mode = 0; mode < 2; ++mode)
     for (int pass = 0; pass < 4; ++pass)
-      for (int tpt : {1, 2, 4, 8})
-        for (int variant : {0, 1, 2, 3}) {
-        const void* k = fb::kernel_for(mode == 1, pass, tpt, variant & 1, variant >= 2);
+      for (int tpt : {1, 2})
+        for (int variant : {0, 1, 2, 3, 4, 5}) {
+        const void* k = fb::kernel_for(mode == 1, pass, tpt, variant % 3, variant >= 3);
         cudaFuncAttributes kfa;
         if (cudaFuncGetAttributes(&kfa, k) != cudaSuccess ||
             cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -455,6 +455,7 @@ namespace {
 struct PlannedLaunch {
   int pass;
   bool mixed;
+  int block;  // CTA size
   int tpt;
   int variant;
   int order;
@@ -513,6 +514,7 @@ void plan_group(Plan& P, const std::vector<DevAtmo>& A, const std::vector<int>& 
     std::memset(&L, 0, sizeof(L));
     L.pass = pass;
     L.mixed = mixed;
+    L.block = pass == fb::kPassDensity ? fb::kDensThreads : fb::kThreads;
     L.tpt = 1;
     L.order = order;
     return L;
@@ -573,16 +575,17 @@ void plan_group(Plan& P, const std::vector<DevAtmo>& A, const std::vector<int>& 
     P.launches.push_back(D);
     PlannedLaunch M = mk(fb::kPassMultiple, n);
     std::vector<int> tm;
+    for (int j : jobs) M.block = std::max(M.block, fb::ms_threads(A[j].W));
     for (int j : jobs) {
       const DevAtmo& a = A[j];
-      tm.push_back(fb::tiles_rows(a.W, a.sc_mu, a.sc_r));
-      M.smem = std::max(M.smem, fb::ms_smem(a.W, a.ms_steps, a.sc_mus, a.sc_nu));
-      M.tpt = std::max(M.tpt, fb::tpt_for_width(a.W));
+      tm.push_back(fb::tiles_multiple(a.W, a.sc_mus, a.ms_steps, a.sc_mu, a.sc_r, M.block));
+      M.smem = std::max(M.smem, fb::ms_smem(a.W, a.ms_steps, a.sc_mus, M.block));
+      M.tpt = std::max(M.tpt, fb::ms_shape(a.W, a.sc_mus, a.ms_steps, M.block).TPT);
       M.texels += (uint64_t)a.W * a.sc_mu * a.sc_r;
     }
     add_segment(P, M, 0, jobs, tm);
     M.nseg = 1;
-    M.variant = launch_variant(A, jobs, tun, mixed, false);
+    M.variant = M.block > fb::kThreads ? 2 : launch_variant(A, jobs, tun, mixed, false);
     P.launches.push_back(M);
   }
 }
@@ -772,7 +775,7 @@ int build(fb_builder* b, cudaStream_t s, const fb_params* params, uint32_t count
       total += L.seg_total[sidx];
     }
     int per_sm = 0;
-    R.block = L.pass == fb::kPassDensity ? fb::kDensThreads : fb::kThreads;
+    R.block = L.block;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, R.fn, R.block, R.smem) != cudaSuccess || per_sm < 1)
       return bail(FB_ERR_CUDA, "occupancy query failed");
     R.args.max_items = std::max(0, max_items_per_cta);

@@ -7,18 +7,14 @@ namespace fb {
 
 template __global__ void k_transmittance<false>(LaunchArgs);
 template __global__ void k_single<false>(LaunchArgs);
+template __global__ void k_multiple<false, 1, 0>(LaunchArgs);
+template __global__ void k_multiple<false, 1, 1>(LaunchArgs);
+template __global__ void k_multiple<false, 1, 2>(LaunchArgs);
+template __global__ void k_multiple<false, 2, 2>(LaunchArgs);
 template __global__ void k_density<false, 0, false>(LaunchArgs);
 template __global__ void k_density<false, 1, false>(LaunchArgs);
 template __global__ void k_density<false, 0, true>(LaunchArgs);
 template __global__ void k_density<false, 1, true>(LaunchArgs);
-template __global__ void k_multiple<false, 1, 0>(LaunchArgs);
-template __global__ void k_multiple<false, 2, 0>(LaunchArgs);
-template __global__ void k_multiple<false, 4, 0>(LaunchArgs);
-template __global__ void k_multiple<false, 8, 0>(LaunchArgs);
-template __global__ void k_multiple<false, 1, 1>(LaunchArgs);
-template __global__ void k_multiple<false, 2, 1>(LaunchArgs);
-template __global__ void k_multiple<false, 4, 1>(LaunchArgs);
-template __global__ void k_multiple<false, 8, 1>(LaunchArgs);
 
 const void* kernel_plain(int pass, int tpt, int variant, bool order2) {
   const bool v1 = variant == 1;
@@ -29,12 +25,8 @@ const void* kernel_plain(int pass, int tpt, int variant, bool order2) {
       if (order2) return v1 ? (const void*)k_density<false, 1, true> : (const void*)k_density<false, 0, true>;
       return v1 ? (const void*)k_density<false, 1, false> : (const void*)k_density<false, 0, false>;
     case kPassMultiple:
-      switch (tpt) {
-        case 1: return v1 ? (const void*)k_multiple<false, 1, 1> : (const void*)k_multiple<false, 1, 0>;
-        case 2: return v1 ? (const void*)k_multiple<false, 2, 1> : (const void*)k_multiple<false, 2, 0>;
-        case 4: return v1 ? (const void*)k_multiple<false, 4, 1> : (const void*)k_multiple<false, 4, 0>;
-        default: return v1 ? (const void*)k_multiple<false, 8, 1> : (const void*)k_multiple<false, 8, 0>;
-      }
+      if (variant == 2) return tpt >= 2 ? (const void*)k_multiple<false, 2, 2> : (const void*)k_multiple<false, 1, 2>;
+      return v1 ? (const void*)k_multiple<false, 1, 1> : (const void*)k_multiple<false, 1, 0>;
   }
   return nullptr;
 }

@@ -69,9 +69,9 @@ int setup_device(int dev, DeviceSetup** out) {
     }
     for (int mode = 0; mode < 2; ++mode)
       for (int pass = 0; pass < 4; ++pass)
-        for (int tpt : {1, 2, 4, 8})
-          for (int order2 = 0; order2 < 2; ++order2) {
-          const void* k = fb::kernel_for(mode == 1, pass, tpt, 0, order2 == 1);
+        for (int tpt : {1, 2})
+          for (int variant : {0, 2, 3}) {
+          const void* k = fb::kernel_for(mode == 1, pass, tpt, variant == 2 ? 2 : 0, variant == 3);
           cudaFuncAttributes fa;
           if (cudaFuncGetAttributes(&fa, k) != cudaSuccess ||
               cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -164,11 +164,11 @@ extern "C" int fb_atmosphere_build_noalloc(void* stream, const fb_params* p, voi
   const int* d_ints = (const int*)(base + o_ints);
   unsigned* d_cnt = (unsigned*)(base + o_cnt);
   std::vector<Launch> L;
-  auto add = [&](int pass, int order, std::vector<int> tiles, size_t smem, int tpt) {
+  auto add = [&](int pass, int order, std::vector<int> tiles, size_t smem, int tpt, int block, int variant) {
     Launch l;
     std::memset(&l, 0, sizeof(l));
-    l.fn = fb::kernel_for(mixed, pass, tpt, 0, order == 2);
-    l.block = pass == fb::kPassDensity ? fb::kDensThreads : fb::kThreads;
+    l.fn = fb::kernel_for(mixed, pass, tpt, variant, order == 2);
+    l.block = block;
     l.smem = smem;
     l.args.atm = d_atm;
     l.args.nseg = (int)tiles.size();
@@ -187,16 +187,18 @@ extern "C" int fb_atmosphere_build_noalloc(void* stream, const fb_params* p, voi
   };
   const bool multi = d.order >= 2;
   add(fb::kPassTransmittance, 0,
-      {fb::tiles_transmittance(d.tr_mu, d.tr_r), fb::tiles_geometry(d.W, d.sc_mu, d.sc_r)}, 0, 1);
+      {fb::tiles_transmittance(d.tr_mu, d.tr_r), fb::tiles_geometry(d.W, d.sc_mu, d.sc_r)}, 0, 1, fb::kThreads, 0);
   add(fb::kPassSingle, 0,
       {fb::tiles_rows(d.W, d.sc_mu, d.sc_r), fb::tiles_direct(d.ir_mus, d.ir_r),
        multi ? fb::tiles_msrec(d.sc_mu, d.sc_r, d.ms_steps) : 0, multi ? fb::tiles_densgeo(d.sc_r, d.dens_n) : 0},
-      fb::ss_smem(d.W, d.ss_steps, d.sc_mus, d.sc_nu), 1);
+      fb::ss_smem(d.W, d.ss_steps, d.sc_mus, d.sc_nu), 1, fb::kThreads, 0);
+  const int ms_block = fb::ms_threads(d.W);
   for (int n = 2; n <= d.order; ++n) {
     const size_t sm = std::max(fb::density_smem(d, n == 2, mixed), fb::indirect_smem(d.irr_n, d.sc_nu, n - 1 == 1));
-    add(fb::kPassDensity, n, {fb::tiles_density(d), fb::tiles_indirect(d.ir_mus, d.ir_r)}, sm, 1);
-    add(fb::kPassMultiple, n, {fb::tiles_rows(d.W, d.sc_mu, d.sc_r)}, fb::ms_smem(d.W, d.ms_steps, d.sc_mus, d.sc_nu),
-        fb::tpt_for_width(d.W));
+    add(fb::kPassDensity, n, {fb::tiles_density(d), fb::tiles_indirect(d.ir_mus, d.ir_r)}, sm, 1, fb::kDensThreads, 0);
+    add(fb::kPassMultiple, n, {fb::tiles_multiple(d.W, d.sc_mus, d.ms_steps, d.sc_mu, d.sc_r, ms_block)},
+        fb::ms_smem(d.W, d.ms_steps, d.sc_mus, ms_block), fb::ms_shape(d.W, d.sc_mus, d.ms_steps, ms_block).TPT, ms_block,
+        ms_block > fb::kThreads ? 2 : 0);
   }
   cudaError_t e = cudaMemcpyAsync(base + o_atm, &d, sizeof(d), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess)

@@ -1239,13 +1239,37 @@ __global__ void __launch_bounds__(kDensThreads, V == 0 ? 4 : 3) k_density(Launch
 // For each sample the CTA interpolates the density table in (mu, r) once into
 // a slab over x; each texel then blends four slab entries (two mu_s
 // neighbours in two nu slices).
-// Slab of one row: W entries plus one guard nu slice (sc_mus entries, zero)
-// read with weight 0 where nu = 1 selects the last slice.
-__host__ __device__ inline int ms_slab_row(int W, int sc_mus) { return W + sc_mus; }
-__host__ __device__ inline size_t ms_smem(int W, int steps, int sc_mus, int sc_nu) {
-  (void)sc_nu;
-  const int R = rows_per_tile(W);
-  return align16(sizeof(MSRec) * (size_t)R * (steps + 1)) + 2 * sizeof(float4) * (size_t)R * ms_slab_row(W, sc_mus);
+// Tile of multiple scattering: whole rows (a texel's lookups can reach any
+// nu slice of its row: its clamped nu picks the slices), R = threads / W rows
+// per CTA for rows of at most `threads` texels, else one row with TPT texels
+// per thread. Launches use CTAs of kThreads threads, or of kMsWideThreads when
+// a row of the launch is wider than kThreads. The slab of a row holds the row
+// plus a zero guard nu slice, read with weight 0 where nu = 1 selects the
+// last slice.
+constexpr int kMsWideThreads = 1024;
+constexpr int kMsRowBytes = 96 * 1024;  // shared memory for the rows of a tile (records + slabs)
+struct MSShape {
+  int R;         // rows per tile
+  int TPT;       // texels per thread
+  int slab_row;  // slab entries per row: W, a zero guard slice and one zero entry
+};
+__host__ __device__ inline MSShape ms_shape(int W, int sc_mus, int steps, int threads) {
+  MSShape m;
+  m.slab_row = W + sc_mus + 1;
+  const int row_bytes = (int)sizeof(MSRec) * (steps + 1) + 2 * (int)sizeof(float4) * m.slab_row;
+  m.R = W <= threads ? min(threads / W, max(1, kMsRowBytes / row_bytes)) : 1;
+  m.TPT = (m.R * W + threads - 1) / threads;
+  return m;
+}
+// CTA size of a launch over rows of width W (the widest of the launch).
+__host__ __device__ inline int ms_threads(int W) { return W <= kThreads ? kThreads : kMsWideThreads; }
+__host__ __device__ inline int tiles_multiple(int W, int sc_mus, int steps, int sc_mu, int sc_r, int threads) {
+  const MSShape m = ms_shape(W, sc_mus, steps, threads);
+  return (sc_mu * sc_r + m.R - 1) / m.R;
+}
+__host__ __device__ inline size_t ms_smem(int W, int steps, int sc_mus, int threads) {
+  const MSShape m = ms_shape(W, sc_mus, steps, threads);
+  return align16(sizeof(MSRec) * (size_t)m.R * (steps + 1)) + 2 * sizeof(float4) * (size_t)m.R * m.slab_row;
 }
 
 // Position t in [0, n - 1] within a row of n texels as (i0, f): texel i0 in
@@ -1262,30 +1286,35 @@ __device__ __forceinline__ int row_pos(float t, float n_minus_1, float& f) {
 
 template <bool MX, int TPT>
 __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned char* smem) {
-  const int W = a.W, nrows = a.sc_mu * a.sc_r;
-  const int R = rows_per_tile(W);
-  const int row0 = tile * R;
-  const int nrow = min(R, nrows - row0);
+  const int W = a.W, nrows = a.sc_mu * a.sc_r, NM = a.sc_mus;
+  const int nth = blockDim.x;
+  const MSShape sh = ms_shape(W, NM, a.ms_steps, nth);
+  const int row0 = tile * sh.R;
+  const int nrow = min(sh.R, nrows - row0);
   const int N = a.ms_steps, NS = N + 1;
   const int tid = threadIdx.x;
+  const int SR = sh.slab_row;                      // slab stride per row
   MSRec* rec = (MSRec*)smem;
-  float4* slab = (float4*)(smem + align16(sizeof(MSRec) * (size_t)R * NS));
-  const int SW = ms_slab_row(W, a.sc_mus);  // slab row stride (W + guard slice)
-  const int slab_n = nrow * W;
-  const int slab_stride = R * SW;
-  for (int k = tid; k < 2 * R * a.sc_mus; k += kThreads) {  // guard slices
-    const int b = k / (R * a.sc_mus), rem = k % (R * a.sc_mus);
-    slab[b * slab_stride + (rem / a.sc_mus) * SW + W + rem % a.sc_mus] = make_float4(0.f, 0.f, 0.f, 0.f);
+  float4* slab = (float4*)(smem + align16(sizeof(MSRec) * (size_t)sh.R * NS));
+  const int nx_tex = nrow * W;                     // texels of the tile = slab entries built per sample
+  const int slab_stride = sh.R * SR;
+  // zero guard after each row: a nu slice (read with weight 0 where nu = 1
+  // selects the last slice) and one entry (read with weight 0 where the mu_s
+  // position is the slice's last texel)
+  const int ng = NM + 1;
+  for (int k = tid; k < 2 * nrow * ng; k += nth) {
+    const int b = k / (nrow * ng), rem = k % (nrow * ng);
+    slab[b * slab_stride + (rem / ng) * SR + W + rem % ng] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
   {  // this tile's sample records
     const int4* src = reinterpret_cast<const int4*>(a.g_ms + (size_t)row0 * NS);
     int4* dst = reinterpret_cast<int4*>(rec);
     const int n16 = nrow * NS * (int)(sizeof(MSRec) / sizeof(int4));
-    for (int k = tid; k < n16; k += kThreads) dst[k] = __ldg(src + k);
+    for (int k = tid; k < n16; k += nth) dst[k] = __ldg(src + k);
   }
-  // per-texel constants (TPT texels per thread)
+  // per-texel constants (TPT texels per thread): row, slab entry, texel x
   float c_rmus[TPT], c_nu[TPT], c_lerp[TPT];
-  int c_lr[TPT], c_x[TPT], c_slice[TPT];
+  int c_lr[TPT], c_e[TPT], c_x[TPT];
   Kahan3 acc[TPT];
   float3 part[TPT];
   MuS32 mus32;
@@ -1297,69 +1326,55 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
     acc[j].init();
     part[j] = make_float3(0.f, 0.f, 0.f);
     c_rmus[j] = c_nu[j] = c_lerp[j] = 0.f;
-    c_slice[j] = 0;
-    const int k = tid + j * kThreads;
+    const int k = tid + j * nth;
     c_lr[j] = k / W;
     c_x[j] = k - c_lr[j] * W;
-    if (k < slab_n) {
+    c_e[j] = c_lr[j] * SR;
+    if (k < nx_tex) {
       float mu_s, nu, rmus;
       texel_mus_nu<MX>(a.g_rows[row0 + c_lr[j]], a.g_cols[c_x[j]], mu_s, nu, rmus);
       c_nu[j] = nu;
       c_rmus[j] = rmus;
-      // scattering.h:146-148
+      // scattering.h:146-148: slices tex_x and tex_x + 1 of the row
       const float tcx = (nu + 1.0f) / 2.0f * float(a.sc_nu - 1);
       const float fl = fminf(fmaxf(floorf(tcx), 0.0f), float(a.sc_nu - 1));
       c_lerp[j] = tcx - fl;
-      c_slice[j] = (int)fl * a.sc_mus;
+      c_e[j] += (int)fl * NM;
     }
   }
   __syncthreads();
   const float4* dens = a.dens;
   const size_t plane = (size_t)a.sc_mu * W;
   // Slab of sample i: the density table interpolated in (mu, r) at the
-  // sample, for every x of the row.
-  float4 nx[TPT][4];
-  auto load = [&](int i) {
+  // sample, for the tile's slices of the row.
+  auto build = [&](int i, float4* dst) {
 #pragma unroll
     for (int j = 0; j < TPT; ++j) {
-      if (tid + j * kThreads < slab_n) {
-        const MSRec& o = rec[c_lr[j] * NS + i];
-        const float4* p0 = dens + o.z0 * plane + c_x[j];
-        const float4* p1 = dens + o.z1 * plane + c_x[j];
-        nx[j][0] = ld4(p0 + (size_t)o.y0 * W);
-        nx[j][1] = ld4(p0 + (size_t)o.y1 * W);
-        nx[j][2] = ld4(p1 + (size_t)o.y0 * W);
-        nx[j][3] = ld4(p1 + (size_t)o.y1 * W);
-      }
+      if (tid + j * nth >= nx_tex) continue;
+      const int lr = c_lr[j], el = c_x[j], x = c_x[j];
+      const MSRec& o = rec[lr * NS + i];
+      const float4* p0 = dens + o.z0 * plane + x;
+      const float4* p1 = dens + o.z1 * plane + x;
+      const float4 a00 = ld4(p0 + (size_t)o.y0 * W), a10 = ld4(p0 + (size_t)o.y1 * W);
+      const float4 a01 = ld4(p1 + (size_t)o.y0 * W), a11 = ld4(p1 + (size_t)o.y1 * W);
+      const float w00 = (1.f - o.fy) * (1.f - o.fz), w10 = o.fy * (1.f - o.fz);
+      const float w01 = (1.f - o.fy) * o.fz, w11 = o.fy * o.fz;
+      float4 v;
+      v.x = fmaf(w11, a11.x, fmaf(w01, a01.x, fmaf(w10, a10.x, w00 * a00.x)));
+      v.y = fmaf(w11, a11.y, fmaf(w01, a01.y, fmaf(w10, a10.y, w00 * a00.y)));
+      v.z = fmaf(w11, a11.z, fmaf(w01, a01.z, fmaf(w10, a10.z, w00 * a00.z)));
+      v.w = 0.f;
+      dst[lr * SR + el] = v;
     }
   };
-  auto store = [&](int i, float4* dst) {
-#pragma unroll
-    for (int j = 0; j < TPT; ++j) {
-      const int k = tid + j * kThreads;
-      if (k < slab_n) {
-        const MSRec& o = rec[c_lr[j] * NS + i];
-        const float w00 = (1.f - o.fy) * (1.f - o.fz), w10 = o.fy * (1.f - o.fz);
-        const float w01 = (1.f - o.fy) * o.fz, w11 = o.fy * o.fz;
-        const float4 a00 = nx[j][0], a10 = nx[j][1], a01 = nx[j][2], a11 = nx[j][3];
-        float4 v;
-        v.x = fmaf(w11, a11.x, fmaf(w01, a01.x, fmaf(w10, a10.x, w00 * a00.x)));
-        v.y = fmaf(w11, a11.y, fmaf(w01, a01.y, fmaf(w10, a10.y, w00 * a00.y)));
-        v.z = fmaf(w11, a11.z, fmaf(w01, a01.z, fmaf(w10, a10.z, w00 * a00.z)));
-        v.w = 0.f;
-        dst[c_lr[j] * SW + c_x[j]] = v;
-      }
-    }
-  };
-  load(0);
-  store(0, slab);
+  build(0, slab);
   __syncthreads();
-  const float fmus = float(a.sc_mus);
+  const float fmus = float(NM);
   for (int i = 0; i < NS; ++i) {
     const float4* cur = slab + (i & 1) * slab_stride;
 #pragma unroll
     for (int j = 0; j < TPT; ++j) {
-      if (tid + j * kThreads < slab_n) {
+      if (tid + j * nth < nx_tex) {
         const MSRec& o = rec[c_lr[j] * NS + i];
         const float nu = c_nu[j];
         // position within a nu slice, texel units (scattering.h:48-56, 149-151):
@@ -1374,9 +1389,8 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
         }
         float fx;
         const int i0 = row_pos(t, fmus - 1.0f, fx);
-        // slices k and k + 1 of the row (k + 1 = nu_size: the zero guard slice)
-        const float4* sl = cur + c_lr[j] * SW + c_slice[j] + i0;
-        const float4 p00 = sl[0], p01 = sl[1], p10 = sl[a.sc_mus], p11 = sl[a.sc_mus + 1];
+        const float4* sl = cur + c_e[j] + i0;
+        const float4 p00 = sl[0], p01 = sl[1], p10 = sl[NM], p11 = sl[NM + 1];
         const float lf = c_lerp[j];
         const float ax = fmaf(p01.x - p00.x, fx, p00.x), bx = fmaf(p11.x - p10.x, fx, p10.x);
         const float ay = fmaf(p01.y - p00.y, fx, p00.y), by = fmaf(p11.y - p10.y, fx, p10.y);
@@ -1395,17 +1409,14 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
         }
       }
     }
-    if (i + 1 < NS) {
-      load(i + 1);
-      store(i + 1, slab + ((i + 1) & 1) * slab_stride);
-    }
+    if (i + 1 < NS) build(i + 1, slab + ((i + 1) & 1) * slab_stride);
     __syncthreads();
   }
   // outputs: delta multiple scattering and the final table (:91-92)
 #pragma unroll
   for (int j = 0; j < TPT; ++j) {
-    const int k = tid + j * kThreads;
-    if (k < slab_n) {
+    const int k = tid + j * nth;
+    if (k < nx_tex) {
       const size_t t = (size_t)(row0 + c_lr[j]) * W + c_x[j];
       const float3 ms = make_float3(acc[j].s.x - acc[j].c.x, acc[j].s.y - acc[j].c.y, acc[j].s.z - acc[j].c.z);
       a.dms[t] = store_round4(make_float4(ms.x, ms.y, ms.z, 0.f), a.f16);
@@ -1432,10 +1443,11 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
   }
 }
 
-// V = 0: registers capped for 4 resident blocks per SM (2 for wide rows);
-// V = 1: for 3 (1 for wide rows).
+// V = 0: CTAs of kThreads, registers capped for 4 resident CTAs per SM;
+// V = 1: for 3; V = 2: CTAs of kMsWideThreads (rows wider than kThreads).
 template <bool MX, int TPT, int V>
-__global__ void __launch_bounds__(kThreads, TPT <= 2 ? (V == 0 ? 4 : 3) : (V == 0 ? 2 : 1)) k_multiple(LaunchArgs L) {
+__global__ void __launch_bounds__(V == 2 ? kMsWideThreads : kThreads, V == 2 ? 1 : (V == 0 ? 4 : 3))
+    k_multiple(LaunchArgs L) {
   extern __shared__ __align__(16) unsigned char smem[];
   int seg, job, tile;
   int taken = 0;

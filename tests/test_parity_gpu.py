@@ -174,3 +174,73 @@ def test_invalid_parameters_rejected_before_launch(builder):
     with pytest.raises(N.FuzzyblueError) as ei:
         Atmosphere.build(builder, smoke_parameters().replace(scattering_mu_size=33))
     assert ei.value.status == N.FB_ERR_INVALID_PARAMS
+
+
+def _wide(**kw):
+    """Rows wider than one CTA of 256 threads: W = nu * mu_s = 16 * 64 = 1024
+    (the layout of the 4x-resolution class), small r and mu so the oracle is fast."""
+    return smoke_parameters(**kw).replace(scattering_nu_size=16, scattering_mu_s_size=64, scattering_r_size=4,
+                                          scattering_mu_size=16)
+
+
+def test_wide_rows_plain_matches_oracle(builder, oracle):
+    p = _wide(order=3)
+    out = gpu_build(builder, p)
+    ref = oracle.precompute(p)
+    _check(out, ref, ("transmittance", "irradiance", "scattering"), PLAIN_MAX, PLAIN_RMS)
+
+
+def test_wide_rows_mixed_matches_fp64(builder, oracle):
+    p = _wide(order=3, precision=PRECISION_MIXED)
+    out = gpu_build(builder, p)
+    ref = oracle.precompute(p, dtype=np.float64)
+    _check(out, ref, ("transmittance", "irradiance", "scattering"), MIXED_MAX)
+
+
+def test_batch_of_mixed_widths_equals_single_builds(builder):
+    """One multiple-scattering launch over rows of 1024 and of 64 texels (CTAs
+    of 1024 threads, four narrow rows per CTA) gives each atmosphere the same
+    bits as its own build."""
+    from fuzzyblue_gb300.api import build_batch
+    ps = [_wide(order=3), smoke_parameters(order=3), _wide(order=2, precision=PRECISION_MIXED),
+          smoke_parameters(order=4, precision=PRECISION_MIXED)]
+    pend = build_batch(builder, ps)
+    pend.wait()
+    outs = [pend.atmosphere(i).to_host() for i in range(len(ps))]
+    pend.release()
+    for p, o in zip(ps, outs):
+        ref = gpu_build(builder, p)
+        for k in ("transmittance", "irradiance", "scattering"):
+            assert np.array_equal(o[k], ref[k]), k
+
+
+@pytest.mark.parametrize("precision", [0, PRECISION_MIXED])
+def test_odd_sizes_match_oracle(builder, oracle, precision):
+    """Sizes the reference's dispatch would leave partly uncomputed (not
+    multiples of its workgroup sizes, src/precompute.rs:1742,1797), odd mu_s
+    and nu sizes included: every texel is computed.
+
+    MIXED meets the FP64 target. PLAIN is held to the accuracy of the
+    reference's own FP32 arithmetic: with a mu_s size that does not divide the
+    packed width exactly, the reference's float texture coordinate of a lookup
+    at a nu-slice boundary can land a fraction of an ulp inside the previous
+    slice, and an exact-weight sampler then blends in that slice's last
+    texel (the sun at the zenith) into a texel at night; the FP32 oracle
+    reproduces it and is up to 18 % away from FP64 here. The kernels keep a
+    lookup inside its slice, so PLAIN must be no farther from FP64 than the
+    FP32 oracle is, and within 3e-2 of the FP32 oracle."""
+    p = smoke_parameters(order=3, precision=precision).replace(
+        scattering_mu_s_size=7, scattering_nu_size=3, scattering_r_size=5, scattering_mu_size=18,
+        transmittance_mu_size=33, transmittance_r_size=9, irradiance_mu_s_size=13, irradiance_r_size=5)
+    out = gpu_build(builder, p)
+    keys = ("transmittance", "irradiance", "scattering")
+    r64 = oracle.precompute(p, dtype=np.float64)
+    if precision == 0:
+        r32 = oracle.precompute(p)
+        _check(out, r32, keys, 3e-2)
+        for k in keys:
+            ours, ref32 = summary(out[k], r64[k]), summary(r32[k].astype(np.float64), r64[k])
+            assert ours["max"] <= max(1.1 * ref32["max"], PLAIN_MAX), (k, ours, ref32)
+            assert ours["rms"] <= max(1.1 * ref32["rms"], PLAIN_RMS), (k, ours, ref32)
+    else:
+        _check(out, r64, keys, MIXED_MAX)
