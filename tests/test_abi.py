@@ -106,3 +106,31 @@ def test_server_config_defaults(native_lib):
     native_lib.fb_server_config_default(ctypes.byref(c))
     assert c.hbm_budget_bytes == 120 << 30
     assert c.max_batch >= 1 and c.max_inflight >= 1 and c.cache_entries >= 1
+
+
+def _rust_sys():
+    return open(os.path.join(ROOT, "rust", "fuzzyblue-cuda-sys", "src", "lib.rs")).read()
+
+
+def test_rust_sys_crate_declares_every_header_function():
+    """The Rust binding (built only where cargo exists) declares every entry
+    point of include/fuzzyblue.h."""
+    import re
+    header = open(os.path.join(ROOT, "include", "fuzzyblue.h")).read()
+    declared = set(re.findall(r"^\s*(?:int|void|const char\*)\s+(fb_[a-z0-9_]+)\(", header, re.M))
+    rust = set(re.findall(r"pub fn (fb_[a-z0-9_]+)\(", _rust_sys()))
+    assert declared and declared == rust, (declared - rust, rust - declared)
+
+
+def test_rust_sys_params_layout_matches_header():
+    """Field order of fb_params_raw / fb_params in the Rust structs is the
+    header's (both are #[repr(C)] / C structs of the same types)."""
+    import re
+    header = open(os.path.join(ROOT, "include", "fuzzyblue.h")).read()
+    rust = _rust_sys()
+    for name in ("fb_params_raw", "fb_params"):
+        hb = re.search(r"typedef struct %s \{(.*?)\} %s;" % (name, name), header, re.S).group(1)
+        hf = re.findall(r"\b(?:float|uint32_t|fb_density_profile|fb_params_raw)\s+(\w+)", hb)
+        rb = re.search(r"pub struct %s \{(.*?)\n\}" % name, rust, re.S).group(1)
+        rf = re.findall(r"pub (\w+):", rb)
+        assert hf == rf, (name, hf, rf)

@@ -1,0 +1,73 @@
+"""LUT export (fuzzyblue_gb300.export): OpenEXR files as the crate's dump
+example writes them (examples/dump.rs:331-367) and NumPy arrays."""
+import struct
+
+import numpy as np
+import pytest
+
+from fuzzyblue_gb300 import export
+from fuzzyblue_gb300.params import smoke_parameters
+
+
+def test_exr_round_trip_and_layout(tmp_path):
+    rng = np.random.default_rng(0)
+    ch = {"R": rng.random((5, 7), dtype=np.float32), "G": rng.random((5, 7), dtype=np.float32),
+          "B": rng.random((5, 7)).astype(np.float16), "ID": np.arange(35, dtype=np.uint32).reshape(5, 7)}
+    path = str(tmp_path / "t.exr")
+    export.write_exr(path, ch)
+    raw = open(path, "rb").read()
+    assert struct.unpack_from("<ii", raw, 0) == (20000630, 2)
+    back, attrs = export.read_exr(path)
+    assert set(back) == set(ch)
+    for k in ch:
+        assert back[k].dtype == ch[k].dtype and np.array_equal(back[k], ch[k]), k
+    assert struct.unpack("<iiii", attrs["dataWindow"]) == (0, 0, 6, 4)
+    assert attrs["compression"] == bytes([0])
+    # channel list sorted by name bytes
+    names = []
+    p = 0
+    while attrs["channels"][p] != 0:
+        e = attrs["channels"].index(b"\0", p)
+        names.append(attrs["channels"][p:e].decode())
+        p = e + 17
+    assert names == sorted(names, key=str.encode)
+
+
+def test_layered_channel_names(tmp_path):
+    t = np.random.default_rng(1).random((12, 3, 4, 4)).astype(np.float16)
+    path = str(tmp_path / "s.exr")
+    export.write_table_exr(path, t)
+    back, _ = export.read_exr(path)
+    assert "10.R" in back and "2.A" in back and len(back) == 48
+    for layer in range(12):
+        for c, color in enumerate("RGBA"):
+            assert np.array_equal(back["%d.%s" % (layer, color)], t[layer, :, :, c])
+    flat = np.random.default_rng(2).random((3, 4, 4), dtype=np.float32)
+    export.write_table_exr(str(tmp_path / "f.exr"), flat)
+    back, _ = export.read_exr(str(tmp_path / "f.exr"))
+    assert sorted(back) == ["A", "B", "G", "R"]
+
+
+@pytest.mark.gpu
+def test_export_atmosphere(builder, tmp_path):
+    from fuzzyblue_gb300.api import Atmosphere
+    pend = Atmosphere.build(builder, smoke_parameters())
+    pend.wait()
+    atm = pend.atmosphere()
+    tables = atm.to_host()
+    half = atm.export_scattering_f16()
+    paths = export.export_atmosphere(atm, str(tmp_path / "exr"))
+    for name in ("transmittance", "irradiance"):
+        back, _ = export.read_exr(paths[name])
+        for c, color in enumerate("RGBA"):
+            assert np.array_equal(back[color], tables[name][..., c]), (name, color)
+    back, _ = export.read_exr(paths["scattering"])
+    depth = tables["scattering"].shape[0]
+    for layer in range(depth):
+        for c, color in enumerate("RGBA"):
+            assert np.array_equal(back["%d.%s" % (layer, color)], half[layer, :, :, c])
+    npy = export.export_atmosphere(atm, str(tmp_path / "npy"), fmt="npy")
+    for name in ("transmittance", "irradiance", "scattering"):
+        assert np.array_equal(np.load(npy[name]), tables[name])
+    assert np.array_equal(np.load(npy["scattering_f16"]), half)
+    pend.release()
