@@ -27,6 +27,12 @@ FB_ERR_SHUTDOWN = -8
 FB_ERR_NO_KERNEL = -9
 
 
+class c_draw_parameters(ctypes.Structure):
+    """fb_draw_parameters: inverse_viewproj[column][row], camera (km), sun direction."""
+    _fields_ = [("inverse_viewproj", (ctypes.c_float * 4) * 4), ("camera_position", ctypes.c_float * 3),
+                ("_pad0", ctypes.c_float), ("sun_direction", ctypes.c_float * 3), ("_pad1", ctypes.c_float)]
+
+
 class c_extent(ctypes.Structure):
     _fields_ = [("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("depth", ctypes.c_uint32)]
 
@@ -144,6 +150,8 @@ SIGNATURES = {
     "fb_atmosphere_destroy": (None, [_V]),
     "fb_batch_build": (_I, [_V, _V, _P, _U32, ctypes.POINTER(_V)]),
     "fb_atmosphere_build_noalloc": (_I, [_V, _P, _V, _V, _V]),
+    "fb_atmosphere_render_sky": (_I, [_V, _V, ctypes.POINTER(c_draw_parameters), _V, _U32, _U32, _V, _V]),
+    "fb_atmosphere_sun_and_sky_irradiance": (_I, [_V, _V, _V, _V, ctypes.POINTER(ctypes.c_float), _U32, _V, _V]),
     "fb_builder_set_profiling": (_I, [_V, _I]),
     "fb_builder_autotune": (_I, [_V, _P, _U32, _U32]),
     "fb_builder_tuned_shape": (_I, [_V, _P, ctypes.POINTER(c_tile_shape)]),

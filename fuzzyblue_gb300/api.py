@@ -190,6 +190,16 @@ class Atmosphere:
                                                    out["scattering"].ctypes.data), "fb_atmosphere_copy_to_host")
         return out
 
+    def render_sky(self, draw, width: int, height: int, depth=None, stream=None):
+        """The crate's sky pass for a width x height image (fuzzyblue_gb300.render)."""
+        from .render import render_sky
+        return render_sky(self, draw, width, height, depth=depth, stream=stream)
+
+    def sun_and_sky_irradiance(self, points, normals, sun_direction, stream=None):
+        """GetSunAndSkyIrradiance at points (fuzzyblue_gb300.render)."""
+        from .render import sun_and_sky_irradiance
+        return sun_and_sky_irradiance(self, points, normals, sun_direction, stream=stream)
+
     def export_scattering_f16(self, stream=None) -> np.ndarray:
         """The scattering table as RGBA16F (np.float16), the reference's image format."""
         sw, sh, sd = self.params.scattering_extent()

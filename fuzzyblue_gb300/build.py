@@ -8,6 +8,7 @@ Translation units are compiled in parallel with nvcc, one -gencode each:
   csrc/fb_serve.cu          request loop with HBM admission and a resident LUT cache
   csrc/fb_tune.cu           tile-shape autotuner
   csrc/fb_noalloc.cu        a build that allocates nothing (fixed device scratch)
+  csrc/fb_render.cu         headless sky pass and surface lighting on the tables, --fmad=false
 """
 import concurrent.futures as cf
 import os
@@ -33,6 +34,7 @@ UNITS = {
     "fb_serve.cu": [],
     "fb_tune.cu": [],
     "fb_noalloc.cu": [],
+    "fb_render.cu": ["--fmad=false"],
 }
 
 

@@ -358,10 +358,46 @@ int fb_server_get_stats(fb_server* s, fb_server_stats* out);
 /* Waits for running batches, frees every resident table, stops the loop. */
 void fb_server_destroy(fb_server* s);
 
+/* ---- headless sky rendering ---------------------------------------------- */
+
+/* The push constants of the crate's sky pass (DrawParameters,
+ * src/render.rs:247-270): (projection * view)^-1 as the columns of a GLSL
+ * mat4 (inverse_viewproj[column][row]), camera position in km and the
+ * direction towards the sun (unit length), in the planet's frame. */
+typedef struct fb_draw_parameters {
+    float inverse_viewproj[4][4];
+    float camera_position[3];
+    float _pad0;
+    float sun_direction[3];
+    float _pad1;
+} fb_draw_parameters;
+
+/* The sky pass of the crate's renderer (render_sky.frag:24-34 over
+ * render_sky.h:111-191) for every pixel of a width x height image, without
+ * a graphics API: pixel (x, y) has screen coordinates ((x + 1/2) / width,
+ * (y + 1/2) / height), `depth` (device, width * height floats, NULL for 0
+ * everywhere: nothing in front of the sky) is the depth the sky pass reads,
+ * world positions are in metres as there and scaled to km. Writes RGBA
+ * float4 per pixel to `color` (radiance, A = 0) and, when not NULL, to
+ * `transmittance` (A = 1), both device memory, rows of `width` pixels. The
+ * tables are sampled as the crate's sampler does (LINEAR, CLAMP_TO_EDGE). */
+int fb_atmosphere_render_sky(const fb_atmosphere* a, void* stream, const fb_draw_parameters* d,
+                             const float* depth, uint32_t width, uint32_t height,
+                             float* color, float* transmittance);
+
+/* GetSunAndSkyIrradiance (render_lighting.h:10-28) at `n` points (km, planet
+ * frame) with surface normals: sun_irradiance and sky_irradiance receive 3
+ * floats per point. All arrays are device memory; sun_direction is 3 floats
+ * of host memory. */
+int fb_atmosphere_sun_and_sky_irradiance(const fb_atmosphere* a, void* stream, const float* points,
+                                         const float* normals, const float* sun_direction, uint32_t n,
+                                         float* sun_irradiance, float* sky_irradiance);
+
 /* ---- profiling ----------------------------------------------------------- */
 
 /* When enabled, builds record a CUDA timing event around every kernel launch
- * (captured into the graph for batches); fb_pending_profile then reports the
+ * (batches then launch directly instead of replaying their CUDA graph: events
+ * inside a graph cannot be read back); fb_pending_profile then reports the
  * device time of each launch once the build has completed. */
 int fb_builder_set_profiling(fb_builder* b, int enabled);
 

@@ -63,11 +63,11 @@ def build_reference(force=False):
         sys.path.pop(0)
     if os.path.isdir(shaders):
         translate.main(["--shaders", shaders, "--out", gen])
-    if not all(os.path.exists(os.path.join(gen, n)) for n in translate.HEADERS + translate.PASSES):
+    if not all(os.path.exists(os.path.join(gen, n)) for n in translate.HEADERS + translate.PASSES + translate.RENDER):
         return None
     runner = os.path.join(HERE, "ref_glsl", "ref_runner.cpp")
     deps = [runner, os.path.join(HERE, "ref_glsl", "glsl_shim.hpp")] + [
-        os.path.join(gen, n) for n in translate.HEADERS + translate.PASSES]
+        os.path.join(gen, n) for n in translate.HEADERS + translate.PASSES + translate.RENDER]
     if force or _stale(REF_SO, deps):
         tmp = REF_SO + ".tmp%d" % os.getpid()
         _run(["g++"] + COMMON + ["-fsingle-precision-constant", "-w",

@@ -482,6 +482,159 @@ template <class T> V3<T> sc_lookup_order(const Atmo<T>& a, const Tab<T>& sr, con
   return sc_lookup(a, ms, r, mu, mu_s, nu, ground);
 }
 
+// ------------------------------------------------------------ render_sky.h ---
+// The renderer's shading (the consumer of the tables): RGBA trilinear fetch,
+// the combined scattering lookup, sky radiance to a point, surface lighting.
+template <class T> struct V4 { T x, y, z, w; };
+template <class T> V4<T> fetch3_rgba(const Tab<T>& t, T u, T v, T s) {
+  int x0, x1, y0, y1, z0, z1;
+  T a, b, c;
+  {
+    SamplerWork<T> not_shader_work;
+    axis(u, t.w, x0, x1, a);
+    axis(v, t.h, y0, y1, b);
+    axis(s, t.d, z0, z1, c);
+  }
+  const T ia = T(1) - a, ib = T(1) - b, ic = T(1) - c;
+  const T w[8] = {ia * ib * ic, a * ib * ic, ia * b * ic, a * b * ic,
+                  ia * ib * c,  a * ib * c,  ia * b * c,  a * b * c};
+  const int xs[2] = {x0, x1}, ys[2] = {y0, y1}, zs[2] = {z0, z1};
+  T acc[4] = {T(0), T(0), T(0), T(0)};
+  for (int k = 0; k < 8; ++k) {
+    const T* p = t.f + 4 * (((size_t)zs[k >> 2] * t.h + ys[(k >> 1) & 1]) * t.w + xs[k & 1]);
+    for (int ch = 0; ch < 4; ++ch) acc[ch] = (k == 0) ? w[k] * p[ch] : acc[ch] + w[k] * p[ch];
+  }
+  return V4<T>{acc[0], acc[1], acc[2], acc[3]};
+}
+template <class T> V3<T> extrapolated_single_mie(const Atmo<T>& a, V4<T> s) {  // render_sky.h:9-19
+  if (s.x <= T(0)) return V3<T>();
+  return V3<T>(s.x, s.y, s.z) * s.w / s.x * (a.rayleigh.x / a.mie_sca.x) * (a.mie_sca / a.rayleigh);
+}
+template <class T>
+V3<T> combined_scattering(const Atmo<T>& a, const Tab<T>& sc, T r, T mu, T mu_s, T nu, bool ground,
+                          V3<T>& single_mie) {  // render_sky.h:21-43
+  Uvwz<T> q = sc_uvwz(a, r, mu, mu_s, nu, ground);
+  T tcx = q.x * T(a.sc_nu - 1);
+  T tex_x = Num<T>::floor(tcx);
+  T lerp = tcx - tex_x;
+  V4<T> s0 = fetch3_rgba(sc, (tex_x + q.y) / T(a.sc_nu), q.z, q.w);
+  V4<T> s1 = fetch3_rgba(sc, (tex_x + T(1) + q.y) / T(a.sc_nu), q.z, q.w);
+  V4<T> m{s0.x * (T(1) - lerp) + s1.x * lerp, s0.y * (T(1) - lerp) + s1.y * lerp,
+          s0.z * (T(1) - lerp) + s1.z * lerp, s0.w * (T(1) - lerp) + s1.w * lerp};
+  single_mie = extrapolated_single_mie(a, m);
+  return V3<T>(m.x, m.y, m.z);
+}
+template <class T> inline T len3(V3<T> v) { return Num<T>::sqrt(dot3(v, v)); }
+// render_sky.h:111-191 (no light shafts: shadow_length 0)
+template <class T>
+V3<T> sky_radiance_to_point(const Atmo<T>& a, const Tab<T>& tr, const Tab<T>& sc, V3<T> camera, V3<T> view,
+                            V3<T> point, V3<T> sun, V3<T>& transmittance) {
+  T r = len3(camera);
+  T rmu = dot3(camera, view);
+  T to_top = -rmu - Num<T>::sqrt(rmu * rmu - r * r + a.top * a.top);
+  if (to_top > T(0)) {
+    camera = camera + view * to_top;
+    r = a.top;
+    rmu = rmu + to_top;
+  } else if (r > a.top) {
+    transmittance = V3<T>::splat(T(1));
+    return V3<T>();
+  }
+  T mu = rmu / r;
+  T mu_s = dot3(camera, sun) / r;
+  T nu = dot3(view, sun);
+  T d = len3(point - camera);
+  bool ground = hits_ground(a, r, mu);
+  transmittance = tr_segment(a, tr, r, mu, d, ground);
+  V3<T> single_mie;
+  V3<T> scattering = combined_scattering(a, sc, r, mu, mu_s, nu, ground, single_mie);
+  if (!std::isinf((double)d)) {
+    T r_p = clamp_radius(a, Num<T>::sqrt(d * d + T(2) * r * mu * d + r * r));
+    T mu_p = (r * mu + d) / r_p;
+    T mu_s_p = (r * mu_s + d * nu) / r_p;
+    V3<T> single_mie_p;
+    V3<T> scattering_p = combined_scattering(a, sc, r_p, mu_p, mu_s_p, nu, ground, single_mie_p);
+    V3<T> shadow = transmittance;
+    scattering = scattering - shadow * scattering_p;
+    single_mie = single_mie - shadow * single_mie_p;
+    single_mie = extrapolated_single_mie(a, V4<T>{scattering.x, scattering.y, scattering.z, single_mie.x});
+    single_mie = single_mie * smoothstep(T(0), T(0.01), mu_s);
+  }
+  return scattering * phase_rayleigh(nu) + single_mie * phase_mie(a.g, nu);
+}
+// render_lighting.h:10-28
+template <class T>
+V3<T> sun_and_sky_irradiance(const Atmo<T>& a, const Tab<T>& tr, const Tab<T>& ir, V3<T> point, V3<T> normal,
+                             V3<T> sun, V3<T>& sky) {
+  T r = len3(point);
+  T mu_s = dot3(point, sun) / r;
+  sky = irr_lookup(a, ir, r, mu_s) * ((T(1) + dot3(normal, point) / r) * T(0.5));
+  return a.solar * tr_to_sun(a, tr, r, mu_s) * gmax(dot3(normal, sun), T(0));
+}
+
+template <class T>
+int render_sky(const fb_params* p, const T* tr, const T* sc, const fb_draw_parameters* d, const T* depth,
+               uint32_t width, uint32_t height, T* color, T* trans) {
+  if (!valid(p) || !tr || !sc || !d || !color || width == 0 || height == 0) return FB_ERR_INVALID_ARGUMENT;
+  const Atmo<T> a = load<T>(p);
+  const Tab<T> ttr{tr, a.tr_mu, a.tr_r, 1}, tsc{sc, a.sc_nu * a.sc_mus, a.sc_mu, a.sc_r};
+  T m[4][4];
+  for (int c = 0; c < 4; ++c)
+    for (int row = 0; row < 4; ++row) m[c][row] = T(d->inverse_viewproj[c][row]);
+  const V3<T> camera = v3<T>(d->camera_position), sun = v3<T>(d->sun_direction);
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int64_t k = 0; k < (int64_t)width * height; ++k) {
+    const uint32_t x = (uint32_t)(k % width), y = (uint32_t)(k / width);
+    // render_sky.frag:24-34
+    const T sx = T(2) * ((T(x) + T(0.5)) / T(width)) - T(1), sy = T(2) * ((T(y) + T(0.5)) / T(height)) - T(1);
+    const T dz = depth ? depth[k] : T(0);
+    T v[4], w[4];
+    for (int row = 0; row < 4; ++row) {
+      v[row] = m[0][row] * sx + m[1][row] * sy + m[2][row] * T(0) + m[3][row] * T(1);
+      w[row] = m[0][row] * sx + m[1][row] * sy + m[2][row] * dz + m[3][row] * T(1);
+    }
+    V3<T> view(v[0], v[1], v[2]);
+    view = view / len3(view);
+    const V3<T> world = (V3<T>(w[0], w[1], w[2]) / w[3]) * T(1e-3);
+    V3<T> t;
+    const V3<T> c = sky_radiance_to_point(a, ttr, tsc, camera, view, world, sun, t);
+    color[4 * k] = c.x;
+    color[4 * k + 1] = c.y;
+    color[4 * k + 2] = c.z;
+    color[4 * k + 3] = T(0);
+    if (trans) {
+      trans[4 * k] = t.x;
+      trans[4 * k + 1] = t.y;
+      trans[4 * k + 2] = t.z;
+      trans[4 * k + 3] = T(1);
+    }
+  }
+  return FB_OK;
+}
+
+template <class T>
+int lighting(const fb_params* p, const T* tr, const T* ir, const T* points, const T* normals, const T* sun_dir,
+             int64_t n, T* sun_out, T* sky_out) {
+  if (!valid(p) || !tr || !ir || !points || !normals || !sun_dir || !sun_out || !sky_out)
+    return FB_ERR_INVALID_ARGUMENT;
+  const Atmo<T> a = load<T>(p);
+  const Tab<T> ttr{tr, a.tr_mu, a.tr_r, 1}, tir{ir, a.ir_mus, a.ir_r, 1};
+  const V3<T> sun(sun_dir[0], sun_dir[1], sun_dir[2]);
+#pragma omp parallel for
+  for (int64_t k = 0; k < n; ++k) {
+    V3<T> sky;
+    const V3<T> direct = sun_and_sky_irradiance(a, ttr, tir, V3<T>(points[3 * k], points[3 * k + 1], points[3 * k + 2]),
+                                                V3<T>(normals[3 * k], normals[3 * k + 1], normals[3 * k + 2]), sun, sky);
+    sun_out[3 * k] = direct.x;
+    sun_out[3 * k + 1] = direct.y;
+    sun_out[3 * k + 2] = direct.z;
+    sky_out[3 * k] = sky.x;
+    sky_out[3 * k + 1] = sky.y;
+    sky_out[3 * k + 2] = sky.z;
+  }
+  return FB_OK;
+}
+
 // ------------------------------------------------------------- the passes ---
 template <class T> inline T store_round(T v, bool f16) {
   if (!f16) return v;
@@ -989,6 +1142,25 @@ void fbo_params_default(fb_params* o) {
 // sqrts, transcendentals, averaged over n sampled texels.
 int fbo_count_ops(const fb_params* p, int pass, int order, int64_t n, uint64_t seed, double* out) {
   return count_ops(p, pass, order, n, seed, out);
+}
+
+int fbo_render_sky_f32(const fb_params* p, const float* tr, const float* sc, const fb_draw_parameters* d,
+                       const float* depth, uint32_t width, uint32_t height, float* color, float* trans) {
+  return render_sky<float>(p, tr, sc, d, depth, width, height, color, trans);
+}
+int fbo_render_sky_f64(const fb_params* p, const double* tr, const double* sc, const fb_draw_parameters* d,
+                       const double* depth, uint32_t width, uint32_t height, double* color, double* trans) {
+  return render_sky<double>(p, tr, sc, d, depth, width, height, color, trans);
+}
+int fbo_sun_and_sky_irradiance_f32(const fb_params* p, const float* tr, const float* ir, const float* points,
+                                   const float* normals, const float* sun, int64_t n, float* sun_out,
+                                   float* sky_out) {
+  return lighting<float>(p, tr, ir, points, normals, sun, n, sun_out, sky_out);
+}
+int fbo_sun_and_sky_irradiance_f64(const fb_params* p, const double* tr, const double* ir, const double* points,
+                                   const double* normals, const double* sun, int64_t n, double* sun_out,
+                                   double* sky_out) {
+  return lighting<double>(p, tr, ir, points, normals, sun, n, sun_out, sky_out);
 }
 
 }  // extern "C"

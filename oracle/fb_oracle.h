@@ -105,6 +105,21 @@ int fbo_multiple_scattering_f64(const fb_params* p, int nthreads,
  * default sample counts, for callers that do not link the library. */
 void fbo_params_default(fb_params* out);
 
+/* The renderer's shading (render_sky.frag:24-34 with render_sky.h:111-191;
+ * render_lighting.h:10-28) on the given tables: see fb_atmosphere_render_sky
+ * and fb_atmosphere_sun_and_sky_irradiance in fuzzyblue.h for the arguments
+ * (host arrays here). */
+int fbo_render_sky_f32(const fb_params* p, const float* tr, const float* sc, const fb_draw_parameters* d,
+                       const float* depth, uint32_t width, uint32_t height, float* color, float* trans);
+int fbo_render_sky_f64(const fb_params* p, const double* tr, const double* sc, const fb_draw_parameters* d,
+                       const double* depth, uint32_t width, uint32_t height, double* color, double* trans);
+int fbo_sun_and_sky_irradiance_f32(const fb_params* p, const float* tr, const float* ir, const float* points,
+                                   const float* normals, const float* sun, int64_t n, float* sun_out,
+                                   float* sky_out);
+int fbo_sun_and_sky_irradiance_f64(const fb_params* p, const double* tr, const double* ir, const double* points,
+                                   const double* normals, const double* sun, int64_t n, double* sun_out,
+                                   double* sky_out);
+
 /* Reference shader arithmetic per texel of one pass (0 transmittance, 1 direct
  * irradiance, 2 single scattering, 3 scattering density of `order`, 4 indirect
  * irradiance of `order`, 5 multiple scattering), averaged over `n` sampled

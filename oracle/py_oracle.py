@@ -18,6 +18,7 @@ ROOT = os.path.dirname(HERE)
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
+from fuzzyblue_gb300._native import c_draw_parameters  # noqa: E402
 from fuzzyblue_gb300.params import Parameters, c_params  # noqa: E402
 from oracle import build as _build  # noqa: E402
 
@@ -51,6 +52,11 @@ def lib():
         L.fbo_multiple_scattering_f64.argtypes = [P, ctypes.c_int, _D, _D, _I, ctypes.c_int64, _D, _D]
         L.fbo_params_default.argtypes = [P]
         L.fbo_count_ops.argtypes = [P, ctypes.c_int, ctypes.c_int, ctypes.c_int64, ctypes.c_uint64, _D]
+        DP = ctypes.POINTER(c_draw_parameters)
+        L.fbo_render_sky_f32.argtypes = [P, _F, _F, DP, _F, ctypes.c_uint32, ctypes.c_uint32, _F, _F]
+        L.fbo_render_sky_f64.argtypes = [P, _D, _D, DP, _D, ctypes.c_uint32, ctypes.c_uint32, _D, _D]
+        L.fbo_sun_and_sky_irradiance_f32.argtypes = [P] + [_F] * 5 + [ctypes.c_int64, _F, _F]
+        L.fbo_sun_and_sky_irradiance_f64.argtypes = [P] + [_D] * 5 + [ctypes.c_int64, _D, _D]
         _lib = L
     return _lib
 
@@ -67,6 +73,9 @@ def ref_lib():
         if path:
             L = ctypes.CDLL(path)
             L.fbref_precompute.argtypes = [ctypes.POINTER(c_params)] + [_F] * 7
+            L.fbref_render_sky.argtypes = [ctypes.POINTER(c_params), _F, _F, ctypes.POINTER(c_draw_parameters), _F,
+                                           ctypes.c_uint32, ctypes.c_uint32, _F, _F]
+            L.fbref_sun_and_sky_irradiance.argtypes = [ctypes.POINTER(c_params)] + [_F] * 5 + [ctypes.c_int64, _F, _F]
             _ref = L
     return _ref
 
@@ -230,4 +239,52 @@ def count_ops(p: Parameters, pass_name: str, order: int = 3, samples: int = 256,
     d = dict(zip(("add", "mul", "div", "sqrt", "transc"), out.tolist()))
     d["flops"] = float(out.sum())
     return d
+
+
+def render_sky(p: Parameters, transmittance, scattering, draw, width, height, depth=None, dtype=np.float32,
+               reference=False):
+    """The sky pass (render_sky.frag over render_sky.h) on host tables:
+    (radiance, transmittance) arrays (height, width, 4). reference=True runs
+    the reference's own shading code compiled as C++ (FP32)."""
+    kind = _F if dtype == np.float32 else _D
+    tr = np.ascontiguousarray(transmittance, dtype)
+    sc = np.ascontiguousarray(scattering, dtype)
+    dep = None if depth is None else np.ascontiguousarray(depth, dtype)
+    color = np.zeros((height, width, 4), dtype)
+    trans = np.zeros((height, width, 4), dtype)
+    c = draw.to_c()
+    if reference:
+        L = ref_lib()
+        if L is None:
+            raise RuntimeError("the reference's shaders are not available")
+        fn = L.fbref_render_sky
+    else:
+        fn = lib().fbo_render_sky_f32 if dtype == np.float32 else lib().fbo_render_sky_f64
+    _check(fn(ctypes.byref(p.to_c()), _ptr(tr, kind), _ptr(sc, kind), ctypes.byref(c), _ptr(dep, kind), width,
+              height, _ptr(color, kind), _ptr(trans, kind)), "render_sky")
+    return color, trans
+
+
+def sun_and_sky_irradiance(p: Parameters, transmittance, irradiance, points, normals, sun_direction,
+                           dtype=np.float32, reference=False):
+    """GetSunAndSkyIrradiance (render_lighting.h) at points (n, 3): (sun, sky) arrays (n, 3)."""
+    kind = _F if dtype == np.float32 else _D
+    tr = np.ascontiguousarray(transmittance, dtype)
+    ir = np.ascontiguousarray(irradiance, dtype)
+    pts = np.ascontiguousarray(points, dtype)
+    nrm = np.ascontiguousarray(normals, dtype)
+    sun = np.ascontiguousarray(sun_direction, dtype)
+    n = pts.shape[0]
+    out_sun = np.zeros((n, 3), dtype)
+    out_sky = np.zeros((n, 3), dtype)
+    if reference:
+        L = ref_lib()
+        if L is None:
+            raise RuntimeError("the reference's shaders are not available")
+        fn = L.fbref_sun_and_sky_irradiance
+    else:
+        fn = lib().fbo_sun_and_sky_irradiance_f32 if dtype == np.float32 else lib().fbo_sun_and_sky_irradiance_f64
+    _check(fn(ctypes.byref(p.to_c()), _ptr(tr, kind), _ptr(ir, kind), _ptr(pts, kind), _ptr(nrm, kind),
+              _ptr(sun, kind), n, _ptr(out_sun, kind), _ptr(out_sky, kind)), "sun_and_sky_irradiance")
+    return out_sun, out_sky
 

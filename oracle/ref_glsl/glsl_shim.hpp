@@ -1,5 +1,6 @@
 // glsl_shim.hpp — the subset of GLSL 4.50 that the reference's compute shaders
-// use, written as C++ so that their unmodified math compiles on the host.
+// and sky-rendering headers use, written as C++ so that their unmodified math
+// compiles on the host.
 //
 // TEST INFRASTRUCTURE ONLY (oracle pinning). Compile with
 // -fsingle-precision-constant (GLSL float literals are single precision) and
@@ -34,7 +35,10 @@ struct vec3 {
   vec3& operator+=(const vec3& o) { x = x + o.x; y = y + o.y; z = z + o.z; return *this; }
 };
 struct vec4 {
-  float x, y, z, w;
+  union { float x; float r; };
+  union { float y; float g; };
+  union { float z; float b; };
+  union { float w; float a; };
   vec4() : x(0), y(0), z(0), w(0) {}
   explicit vec4(float s) : x(s), y(s), z(s), w(s) {}
   vec4(float a, float b, float c, float d) : x(a), y(b), z(c), w(d) {}
@@ -94,6 +98,12 @@ inline float smoothstep(float e0, float e1, float x) {
 }
 inline float dot(const vec3& a, const vec3& b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 inline vec3 normalize(const vec3& v) { return v / std::sqrt(dot(v, v)); }
+inline float length(const vec3& v) { return std::sqrt(dot(v, v)); }
+inline vec4 mix(const vec4& x, const vec4& y, float t) {
+  return vec4(x.x * (1.0f - t) + y.x * t, x.y * (1.0f - t) + y.y * t, x.z * (1.0f - t) + y.z * t,
+              x.w * (1.0f - t) + y.w * t);
+}
+inline bool isinf(float x) { return std::isinf(x); }
 inline bvec2 greaterThanEqual(const uvec2& a, const uvec2& b) { return {a.x >= b.x, a.y >= b.y}; }
 inline bvec3 greaterThanEqual(const uvec3& a, const uvec3& b) { return {a.x >= b.x, a.y >= b.y, a.z >= b.z}; }
 inline bool any(const bvec2& v) { return v.x || v.y; }

@@ -31,6 +31,10 @@ namespace p_indirect {
 namespace p_multiple {
 #include "multiple_scattering.comp"
 }
+namespace p_render {
+#include "render_sky.h"
+#include "render_lighting.h"
+}
 }  // namespace glsl
 
 #include <cstring>
@@ -258,6 +262,76 @@ int fbref_run_pass(int pass, const fb_params* p, int order, float* tr, float* di
   for (int64_t k = 0; k < n; ++k) {
     const int64_t id = ids[k];
     entry(uvec3((uint)(id % w), (uint)((id / w) % h), (uint)(id / (w * h))));
+  }
+  return FB_OK;
+}
+
+// The sky pass of the crate's renderer: render_sky.frag:24-34 per pixel with
+// the reference's GetSkyRadianceToPoint (render_sky.h, compiled as C++).
+// Screen coordinates are pixel centres; depth NULL reads 0 everywhere.
+int fbref_render_sky(const fb_params* p, const float* tr, const float* sc, const fb_draw_parameters* d,
+                     const float* depth, uint32_t width, uint32_t height, float* color, float* transmittance) {
+  if (!p || !tr || !sc || !d || !color || width == 0 || height == 0) return FB_ERR_INVALID_ARGUMENT;
+  const fb_params_raw& r = p->raw;
+  const AtmosphereParameters atm = convert(r);
+  const sampler2D s_tr = {tr, (int)r.transmittance_mu_size, (int)r.transmittance_r_size};
+  const sampler3D s_sc = {sc, (int)(r.scattering_nu_size * r.scattering_mu_s_size), (int)r.scattering_mu_size,
+                          (int)r.scattering_r_size};
+  const float(*m)[4] = d->inverse_viewproj;
+  // mat4 (columns m[c]) times vec4
+  auto mul = [&](float x, float y, float z, float w, float out[4]) {
+    for (int row = 0; row < 4; ++row) out[row] = m[0][row] * x + m[1][row] * y + m[2][row] * z + m[3][row] * w;
+  };
+  const vec3 camera(d->camera_position[0], d->camera_position[1], d->camera_position[2]);
+  const vec3 sun(d->sun_direction[0], d->sun_direction[1], d->sun_direction[2]);
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int64_t k = 0; k < (int64_t)width * height; ++k) {
+    const uint32_t x = (uint32_t)(k % width), y = (uint32_t)(k / width);
+    const vec2 screen((x + 0.5f) / (float)width, (y + 0.5f) / (float)height);
+    const float sx = 2 * screen.x - 1, sy = 2 * screen.y - 1;
+    float v[4], wp[4];
+    mul(sx, sy, 0, 1, v);
+    const vec3 view = normalize(vec3(v[0], v[1], v[2]));
+    mul(sx, sy, depth ? depth[k] : 0.0f, 1, wp);
+    const vec3 world = (vec3(wp[0], wp[1], wp[2]) / wp[3]) * 1e-3f;
+    vec3 t;
+    const vec3 c = p_render::GetSkyRadianceToPoint(atm, s_tr, s_sc, camera, view, world, sun, t);
+    color[4 * k] = c.x;
+    color[4 * k + 1] = c.y;
+    color[4 * k + 2] = c.z;
+    color[4 * k + 3] = 0.0f;
+    if (transmittance) {
+      transmittance[4 * k] = t.x;
+      transmittance[4 * k + 1] = t.y;
+      transmittance[4 * k + 2] = t.z;
+      transmittance[4 * k + 3] = 1.0f;
+    }
+  }
+  return FB_OK;
+}
+
+// GetSunAndSkyIrradiance (render_lighting.h) at n points.
+int fbref_sun_and_sky_irradiance(const fb_params* p, const float* tr, const float* ir, const float* points,
+                                 const float* normals, const float* sun_direction, int64_t n, float* sun_out,
+                                 float* sky_out) {
+  if (!p || !tr || !ir || !points || !normals || !sun_direction || !sun_out || !sky_out)
+    return FB_ERR_INVALID_ARGUMENT;
+  const fb_params_raw& r = p->raw;
+  const AtmosphereParameters atm = convert(r);
+  const sampler2D s_tr = {tr, (int)r.transmittance_mu_size, (int)r.transmittance_r_size};
+  const sampler2D s_ir = {ir, (int)r.irradiance_mu_s_size, (int)r.irradiance_r_size};
+  const vec3 sun(sun_direction[0], sun_direction[1], sun_direction[2]);
+#pragma omp parallel for
+  for (int64_t k = 0; k < n; ++k) {
+    vec3 sky;
+    const vec3 direct = p_render::GetSunAndSkyIrradiance(atm, s_tr, s_ir, v3(points + 3 * k), v3(normals + 3 * k),
+                                                         sun, sky);
+    sun_out[3 * k] = direct.x;
+    sun_out[3 * k + 1] = direct.y;
+    sun_out[3 * k + 2] = direct.z;
+    sky_out[3 * k] = sky.x;
+    sky_out[3 * k + 1] = sky.y;
+    sky_out[3 * k + 2] = sky.z;
   }
   return FB_OK;
 }

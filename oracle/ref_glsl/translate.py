@@ -1,8 +1,10 @@
-"""Mechanical GLSL -> C++ rewrite of the reference's compute shaders.
+"""Mechanical GLSL -> C++ rewrite of the reference's compute shaders and of its
+sky-rendering headers.
 
 TEST INFRASTRUCTURE ONLY (oracle pinning). Reads the reference's shader
 sources where they lie (shaders/util.h, params.h, transmittance.h,
-irradiance.h, scattering.h and the six precompute *.comp files) and writes
+irradiance.h, scattering.h, the six precompute *.comp files, render_sky.h and
+render_lighting.h) and writes
 compilable C++ copies into oracle/_ref/gen/ (git-ignored), never into the
 repository. The rewrite is purely syntactic, so the arithmetic compiled is the
 reference's own:
@@ -23,6 +25,8 @@ import re
 import sys
 
 HEADERS = ["util.h", "params.h", "transmittance.h", "irradiance.h", "scattering.h"]
+# the renderer's shading functions (render_sky.frag includes render_sky.h)
+RENDER = ["render_sky.h", "render_lighting.h"]
 PASSES = [
     "transmittance.comp",
     "direct_irradiance.comp",
@@ -61,7 +65,7 @@ def main(argv=None) -> int:
     ap.add_argument("--out", required=True, help="output directory (oracle/_ref/gen)")
     a = ap.parse_args(argv)
     os.makedirs(a.out, exist_ok=True)
-    for name in HEADERS + PASSES:
+    for name in HEADERS + PASSES + RENDER:
         with open(os.path.join(a.shaders, name)) as f:
             text = f.read()
         with open(os.path.join(a.out, name), "w") as f:

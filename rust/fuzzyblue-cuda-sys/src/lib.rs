@@ -161,6 +161,17 @@ pub struct fb_launch_profile {
 pub type fb_alloc_fn = Option<unsafe extern "C" fn(user: *mut c_void, bytes: usize, stream: *mut c_void) -> *mut c_void>;
 pub type fb_free_fn = Option<unsafe extern "C" fn(user: *mut c_void, ptr: *mut c_void, stream: *mut c_void)>;
 
+/// Push constants of the crate's sky pass: inverse_viewproj[column][row].
+#[repr(C)]
+#[derive(Clone, Copy, Debug, Default)]
+pub struct fb_draw_parameters {
+    pub inverse_viewproj: [[f32; 4]; 4],
+    pub camera_position: [f32; 3],
+    pub _pad0: f32,
+    pub sun_direction: [f32; 3],
+    pub _pad1: f32,
+}
+
 #[repr(C)]
 #[derive(Clone, Copy, Debug, Default)]
 pub struct fb_server_config {
@@ -236,6 +247,13 @@ extern "C" {
     pub fn fb_atmosphere_destroy(a: *mut fb_atmosphere);
     pub fn fb_atmosphere_build_noalloc(stream: *mut c_void, p: *const fb_params, transmittance: *mut c_void,
                                        irradiance: *mut c_void, scattering: *mut c_void) -> c_int;
+
+    pub fn fb_atmosphere_render_sky(a: *const fb_atmosphere, stream: *mut c_void, d: *const fb_draw_parameters,
+                                    depth: *const f32, width: u32, height: u32, color: *mut f32,
+                                    transmittance: *mut f32) -> c_int;
+    pub fn fb_atmosphere_sun_and_sky_irradiance(a: *const fb_atmosphere, stream: *mut c_void, points: *const f32,
+                                                normals: *const f32, sun_direction: *const f32, n: u32,
+                                                sun_irradiance: *mut f32, sky_irradiance: *mut f32) -> c_int;
 
     pub fn fb_server_config_default(out: *mut fb_server_config);
     pub fn fb_server_create(b: *mut fb_builder, cfg: *const fb_server_config, out: *mut *mut fb_server) -> c_int;

@@ -249,6 +249,15 @@ impl Parameters {
     }
 }
 
+/// The crate's `DrawParameters` (src/render.rs:247-252).
+#[derive(Clone, Copy, Debug, PartialEq)]
+pub struct DrawParameters {
+    /// (projection * view)^-1
+    pub inverse_viewproj: [[f32; 4]; 4],
+    pub camera_position: [f32; 3],
+    pub sun_direction: [f32; 3],
+}
+
 /// A CUDA device with the precompute kernels loaded (the crate's `Builder`).
 pub struct Builder {
     raw: *mut sys::fb_builder,
@@ -355,6 +364,22 @@ impl Atmosphere {
             sys::fb_atmosphere_copy_to_host(self.raw, ptr::null_mut(), t.as_mut_ptr(), i.as_mut_ptr(), s.as_mut_ptr())
         })?;
         Ok((t, i, s))
+    }
+
+    /// The crate's sky pass (render_sky.frag) for a width x height image into
+    /// device buffers of RGBA f32 (`transmittance` may be null); `depth` is a
+    /// device buffer of width * height floats or null (nothing in front of the sky).
+    pub unsafe fn render_sky(&self, stream: Stream, draw: &DrawParameters, depth: *const f32, width: u32,
+                             height: u32, color: *mut f32, transmittance: *mut f32) -> Result<(), Error> {
+        let d = sys::fb_draw_parameters {
+            inverse_viewproj: draw.inverse_viewproj,
+            camera_position: draw.camera_position,
+            _pad0: 0.0,
+            sun_direction: draw.sun_direction,
+            _pad1: 0.0,
+        };
+        check(sys::fb_atmosphere_render_sky(self.raw, stream.0, &d, depth, width, height, color, transmittance))
+            .map(|_| ())
     }
 
     /// The scattering table as RGBA16F bits (the crate's image format).

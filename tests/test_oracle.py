@@ -163,3 +163,50 @@ def test_op_count_of_branch_free_passes_is_exact(oracle):
     assert d2["flops"] > d3["flops"] > 512 * 50
     # 16 x 64 hemisphere directions, one transcendental-free table lookup each
     assert a["transc"] == 0 and a["sqrt"] == 4 * 1024
+
+
+def _camera(seed):
+    from fuzzyblue_gb300.render import DrawParameters
+    rng = np.random.default_rng(seed)
+    fwd = rng.normal(size=3)
+    fwd[1] = abs(fwd[1]) * 0.3
+    sun = rng.normal(size=3)
+    return DrawParameters.look_at((0.0, 6360.5 + 3.0 * seed, 0.0), forward=fwd, up=(0, 1, 0), fov_y_deg=75,
+                                  aspect=1.5, sun_direction=sun)
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_oracle_sky_pass_matches_reference_shaders(oracle, seed):
+    """The oracle's restatement of the sky pass (render_sky.frag over
+    render_sky.h) equals the reference's own shading code compiled as C++,
+    bit for bit (NaN where the reference gives NaN: the transmittance of
+    downward rays to an infinitely far point)."""
+    if oracle.ref_lib() is None:
+        pytest.skip("the reference's shaders are not available")
+    p = smoke_parameters()
+    t = oracle.precompute(p)
+    d = _camera(seed)
+    rng = np.random.default_rng(seed)
+    depth = np.where(rng.random((24, 36)) < 0.3, rng.uniform(1e-5, 1e-2, (24, 36)), 0.0).astype(np.float32)
+    for dep in (None, depth):
+        c1, t1 = oracle.render_sky(p, t["transmittance"], t["scattering"], d, 36, 24, depth=dep)
+        c2, t2 = oracle.render_sky(p, t["transmittance"], t["scattering"], d, 36, 24, depth=dep, reference=True)
+        assert np.array_equal(c1, c2, equal_nan=True) and np.array_equal(t1, t2, equal_nan=True)
+        assert np.isfinite(c1).mean() > 0.9
+
+
+def test_oracle_lighting_matches_reference_shaders(oracle):
+    if oracle.ref_lib() is None:
+        pytest.skip("the reference's shaders are not available")
+    p = smoke_parameters()
+    t = oracle.precompute(p)
+    rng = np.random.default_rng(3)
+    dirs = rng.normal(size=(500, 3))
+    dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+    pts = dirs * rng.uniform(p.bottom_radius, p.top_radius, (500, 1))
+    nrm = rng.normal(size=(500, 3))
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    sun = np.array([0.2, 0.9, 0.1]) / np.linalg.norm([0.2, 0.9, 0.1])
+    a = oracle.sun_and_sky_irradiance(p, t["transmittance"], t["irradiance"], pts, nrm, sun)
+    b = oracle.sun_and_sky_irradiance(p, t["transmittance"], t["irradiance"], pts, nrm, sun, reference=True)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
