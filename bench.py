@@ -522,6 +522,13 @@ def run_uneven(a):
 
 
 # ---------------------------------------------------------------- serving ---
+def _class_percentiles(lat):
+    """{class: {"n", "p50_ms", "p99_ms"}} of per-class latency arrays (ms)."""
+    import numpy as np
+    return {c: {"n": int(len(v)), "p50_ms": float(np.percentile(v, 50)) if len(v) else None,
+                "p99_ms": float(np.percentile(v, 99)) if len(v) else None} for c, v in lat.items()}
+
+
 def run_serve(a):
     """Open-loop Poisson request stream (seed 2) through the request loop
     (fb_server_*): each request one atmosphere drawn from the uniform-batch
@@ -540,7 +547,8 @@ def run_serve(a):
     from fuzzyblue_gb300.params import PRECISION_MIXED, PRECISION_PLAIN
     builder = Builder(0)
     names = ("default", "half", "double")
-    probe = workloads.draw_atmosphere(np.random.default_rng(99), precision=PRECISION_MIXED)
+    prec = PRECISION_MIXED if a.precision == "mixed" else PRECISION_PLAIN
+    probe = workloads.draw_atmosphere(np.random.default_rng(99), precision=prec)
     if not a.no_autotune:
         builder.autotune([probe.replace(**workloads.CLASSES[c]) for c in names], batch=4)
 
@@ -572,9 +580,9 @@ def run_serve(a):
             if t > a.duration:
                 break
             arrivals.append(t)
-        reqs = [workloads.serving_request(rng) for _ in arrivals]
+        reqs = [workloads.serving_request(rng, precision=prec) for _ in arrivals]
         srv = Server(builder, hbm_budget_bytes=120 * 10 ** 9, max_queue=a.max_queue)
-        submit_at, done_at, rejected, fresh = {}, {}, [0], []
+        submit_at, done_at, rejected, fresh, cls_at = {}, {}, [0], [], {}
         lock = threading.Lock()
         start = time.perf_counter() + 0.05
 
@@ -591,6 +599,7 @@ def run_serve(a):
                     continue
                 with lock:
                     submit_at[tk] = start + at
+                    cls_at[tk] = cls_of(p)
                     fresh.append(tk)
         th = threading.Thread(target=submitter)
         th.start()
@@ -617,15 +626,18 @@ def run_serve(a):
         st = srv.stats()
         srv.close()
         lat = np.array([done_at[k] - submit_at[k] for k in done_at]) * 1e3
+        lat_cls = {c: np.array([done_at[k] - submit_at[k] for k in done_at if cls_at[k] == c]) * 1e3 for c in names}
         end = max(done_at.values()) if done_at else start
         served = {"completed": len(done_at), "rejected": rejected[0],
                   "throughput": len(done_at) / max(end - start, 1e-9),
                   "p50_ms": float(np.percentile(lat, 50)) if len(lat) else None,
                   "p99_ms": float(np.percentile(lat, 99)) if len(lat) else None,
                   "server_p50_ms": st["p50_ms"], "server_p99_ms": st["p99_ms"], "batches": st["batches"],
-                  "mean_batch": st["mean_batch"], "evictions": st["evictions"]}
+                  "mean_batch": st["mean_batch"], "evictions": st["evictions"],
+                  "by_class": _class_percentiles(lat_cls)}
         # the plain path on the same arrivals: one FIFO server, same queue limit
         free_at, lat_p, comp, rej_p, queue = 0.0, [], 0, 0, []
+        lat_pc = {c: [] for c in names}
         for at, p in zip(arrivals, reqs):
             queue = [x for x in queue if x > at]  # completion times still ahead
             if len(queue) > a.max_queue:
@@ -636,20 +648,22 @@ def run_serve(a):
             free_at = begin + s_t
             queue.append(free_at)
             lat_p.append((free_at - at) * 1e3)
+            lat_pc[cls_of(p)].append(lat_p[-1])
             comp += 1
         plain = {"completed": comp, "rejected": rej_p, "throughput": comp / max(free_at, 1e-9),
-                 "p50_ms": float(np.percentile(lat_p, 50)), "p99_ms": float(np.percentile(lat_p, 99))}
+                 "p50_ms": float(np.percentile(lat_p, 50)), "p99_ms": float(np.percentile(lat_p, 99)),
+                 "by_class": _class_percentiles({c: np.array(v) for c, v in lat_pc.items()})}
         lines.append({"offered_rate": rate, "requests": len(arrivals), "served": served, "plain": plain,
                       "served_over_plain_throughput": served["throughput"] / plain["throughput"]})
     out = {
         "metric": "served atmospheres/s and p50/p99 request latency, Poisson open loop",
         "value": max(l["served"]["throughput"] for l in lines), "unit": "atmospheres/s", "n_gpus": 1,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 with f64 ray geometry and order accumulation",
+        "dtype": "f32 with f64 ray geometry and order accumulation" if a.precision == "mixed" else "f32",
         "data": "synthetic: seeded requests (fuzzyblue_gb300.workloads.serving_request, seed 2)",
         "config": {"workload": "serving: open-loop Poisson requests, class 60/30/10 default / half / double, "
                                "orders 2-8, 120 GB HBM budget, LRU-resident tables",
-                   "duration_s": a.duration, "max_queue": a.max_queue,
+                   "duration_s": a.duration, "max_queue": a.max_queue, "precision": a.precision,
                    "plain_path": "plain FP32 single builds per (class, order), measured, replayed FIFO"},
         "rates": lines,
     }

@@ -6,12 +6,17 @@
 // One scheduler thread owns every CUDA call of the server. Each pass of its
 // loop (1) collects finished batches (a host callback after each batch wakes
 // it), moving their tables into the resident cache and freeing their
-// temporaries; (2) while a stream is free, takes the oldest queued request
-// and every queued request of its table class, in arrival order, while the
-// budget allows (evicting unpinned resident tables, least recently used
-// first), and launches them as one batch build - cheap batches on
-// high-priority streams, with CTAs that exit after a few work items so that
-// they interleave with a long build already running; (3) sleeps until woken.
+// temporaries; (2) while a stream is free, picks the request that leads its
+// batch - on a high-priority stream the oldest cheap request, on a
+// low-priority stream the oldest request of any class - adds the queued
+// requests of the lead's table class in arrival order while the budget
+// (evicting unpinned resident tables, least recently used first) and the
+// batch's estimated duration allow, and launches them as one batch build
+// whose CTAs exit after a few work items, so that a cheap batch's kernels
+// are dispatched ahead of a long build already running; while a long build
+// has run well past its estimated duration, cheap batches keep to the
+// low-priority streams beside it, and a request queued for over a second
+// leads the next batch on any stream; (3) sleeps until woken.
 // Requests for parameters already resident or in flight share that result.
 #include <cuda_runtime.h>
 
@@ -68,6 +73,8 @@ struct Batch {
   int stream_slot = -1;
   std::vector<Entry*> entries;
   size_t bytes = 0;
+  double cost = 0;      // texel-orders
+  double t_launch = 0;  // ms
   bool has_callback = false;      // completion is signalled by the host callback
   std::atomic<bool> done{false};  // set by that callback as its last action
 };
@@ -101,6 +108,7 @@ struct fb_server {
   std::vector<bool> stream_busy;
   std::vector<bool> stream_high;  // high-priority stream (cheap batches)
   size_t resident_bytes = 0, inflight_bytes = 0;
+  double rate = 0;  // best texel-orders per ms seen over a finished batch (0: none yet)
   uint64_t next_ticket = 1, clock = 0;
   fb_server_stats st;
   std::vector<double> lat;
@@ -187,6 +195,8 @@ void collect(fb_server* s) {
       e->waiters.clear();
     }
     s->inflight_bytes -= bt->bytes;
+    const double took = now_ms() - bt->t_launch;
+    if (took > 0) s->rate = std::max(s->rate, bt->cost / took);
     fbi::pending_destroy(bt->pending);
     s->stream_busy[bt->stream_slot] = false;
     delete bt;
@@ -212,48 +222,126 @@ bool same_class(const fb_params& a, const fb_params& b) {
 }
 // Batches up to this cost (texel-orders) run on the high-priority streams.
 constexpr double kCheapBatch = 1048576.0 * 8;
+// Starvation guard: a batch on a low-priority stream that has run longer than
+// kStarveFactor times its estimated duration (its cost at the best throughput
+// seen so far) plus kStarveSlackMs holds new cheap batches off the
+// high-priority streams until it finishes; they then share the low-priority
+// streams with it, where the block scheduler serves kernels in launch order.
+constexpr double kStarveFactor = 2.0;
+constexpr double kStarveSlackMs = 20.0;
+constexpr double kInitialRate = 1.0e6;  // texel-orders per ms before any batch finished
+// A batch takes further requests only while its estimated duration stays
+// under this: one atmosphere of the default class already fills the GPU, so
+// larger batches gain little throughput while every request in them waits
+// for the whole batch.
+constexpr double kBatchTargetMs = 100.0;
 
-// Drops queue entries that no longer wait (cancelled, or shared with a
-// resident / in-flight result) from the front.
-bool settle_head(fb_server* s) {
-  while (!s->queue.empty()) {
-    const uint64_t t = s->queue.front();
+bool low_priority_starved(const fb_server* s, double now) {
+  const double rate = s->rate > 0 ? s->rate : kInitialRate;
+  for (const Batch* bt : s->inflight)
+    if (!s->stream_high[bt->stream_slot] && now - bt->t_launch > kStarveFactor * bt->cost / rate + kStarveSlackMs)
+      return true;
+  return false;
+}
+
+// Answers a queued request from a resident or in-flight result with the same
+// parameters; true if there was one.
+bool share_result(fb_server* s, uint64_t t, Request& r) {
+  auto ex = s->entries.find(r.key);
+  if (ex == s->entries.end()) return false;
+  s->st.cache_hits++;
+  if (ex->second->ready) complete_request(s, t, ex->second);
+  else {
+    r.state = State::Running;
+    ex->second->waiters.push_back(t);
+  }
+  return true;
+}
+
+// Queue entries looked at for the request that leads a batch.
+constexpr size_t kLeadScan = 4096;
+// Aging: a request queued longer than this leads the next batch on any free
+// stream, whatever its class. Under overload this serves the queue in
+// arrival order, so that cheap requests cannot hold an expensive one back
+// without bound; at moderate load no request waits that long.
+constexpr double kUrgentMs = 1000.0;
+
+// Picks a free stream and the request that leads its batch: a high-priority
+// stream takes the oldest cheap request (none while a long batch is held
+// back), a low-priority stream the oldest request of any class; with no
+// low-priority stream at all the high-priority ones take everything. The
+// oldest request, once urgent (kUrgentMs), takes any free stream.
+// Drops cancelled and shared entries met on the way. `cheap_only`: the batch
+// may hold cheap requests only.
+bool pick_lead(fb_server* s, int& slot, uint64_t& lead, bool& cheap_only) {
+  int free_high = -1, free_low = -1;
+  bool any_low = false;
+  for (size_t k = 0; k < s->streams.size(); ++k) {
+    any_low |= !s->stream_high[k];
+    if (s->stream_busy[k]) continue;
+    if (s->stream_high[k]) {
+      if (free_high < 0) free_high = (int)k;
+    } else if (free_low < 0) {
+      free_low = (int)k;
+    }
+  }
+  if (free_high < 0 && free_low < 0) return false;
+  const double now = now_ms();
+  const bool high_for_all = !any_low;
+  const bool hold_high = !high_for_all && low_priority_starved(s, now);
+  size_t seen = 0;
+  bool oldest = true;
+  for (auto qi = s->queue.begin(); qi != s->queue.end() && seen < kLeadScan;) {
+    const uint64_t t = *qi;
     auto it = s->reqs.find(t);
     if (it == s->reqs.end() || it->second.state != State::Queued) {
-      s->queue.pop_front();
+      qi = s->queue.erase(qi);
       continue;
     }
-    Request& r = it->second;
-    auto ex = s->entries.find(r.key);
-    if (ex == s->entries.end()) return true;
-    s->st.cache_hits++;
-    s->queue.pop_front();
-    if (ex->second->ready) complete_request(s, t, ex->second);
-    else {
-      r.state = State::Running;
-      ex->second->waiters.push_back(t);
+    if (share_result(s, t, it->second)) {
+      qi = s->queue.erase(qi);
+      continue;
     }
+    if (oldest && now - it->second.t_submit > kUrgentMs) {
+      slot = free_high >= 0 ? free_high : free_low;
+      lead = t;
+      cheap_only = false;
+      return true;
+    }
+    oldest = false;
+    if (free_low < 0 && hold_high) return false;
+    const bool cheap = cost_of(it->second.params) <= kCheapBatch;
+    if (free_high >= 0 && (high_for_all || (cheap && !hold_high))) {
+      slot = free_high;
+      lead = t;
+      cheap_only = !high_for_all;
+      return true;
+    }
+    if (free_low >= 0) {
+      slot = free_low;
+      lead = t;
+      cheap_only = false;
+      return true;
+    }
+    ++qi;
+    ++seen;
   }
   return false;
 }
 
 void admit(fb_server* s) {
-  while (settle_head(s)) {
-    const fb_params head = s->reqs[s->queue.front()].params;
-    // the head request's class, then every queued request of that class in
-    // arrival order (shared results are settled as they are met)
-    const bool cheap = cost_of(head) <= kCheapBatch;
-    int slot = -1;
-    for (int pass = 0; pass < 2 && slot < 0; ++pass)
-      for (size_t k = 0; k < s->streams.size(); ++k)
-        if (!s->stream_busy[k] && (pass == 1 || s->stream_high[k] == cheap)) {
-          slot = (int)k;
-          break;
-        }
-    if (slot < 0) return;
+  int slot;
+  uint64_t lead;
+  bool cheap_only;
+  while (pick_lead(s, slot, lead, cheap_only)) {
+    // the lead request, then the queued requests of its class in arrival
+    // order (shared results are settled as they are met)
+    const fb_params head = s->reqs[lead].params;
+    const double cost_cap = kBatchTargetMs * (s->rate > 0 ? s->rate : kInitialRate);
     Batch* bt = new Batch();
     std::vector<fb_params> params;
     size_t bytes = 0;
+    double cost = 0;
     bool full = false;
     for (auto qi = s->queue.begin(); qi != s->queue.end() && params.size() < s->cfg.max_batch && !full;) {
       const uint64_t t = *qi;
@@ -263,21 +351,15 @@ void admit(fb_server* s) {
         continue;
       }
       Request& r = it->second;
-      if (!same_class(r.params, head)) {
+      if (!same_class(r.params, head) || (cheap_only && cost_of(r.params) > kCheapBatch)) {
         ++qi;
         continue;
       }
-      auto ex = s->entries.find(r.key);
-      if (ex != s->entries.end()) {  // resident or in flight: share it
-        s->st.cache_hits++;
+      if (share_result(s, t, r)) {  // resident or in flight: share it
         qi = s->queue.erase(qi);
-        if (ex->second->ready) complete_request(s, t, ex->second);
-        else {
-          r.state = State::Running;
-          ex->second->waiters.push_back(t);
-        }
         continue;
       }
+      if (!params.empty() && cost + cost_of(r.params) > cost_cap) break;
       if (s->resident_bytes + s->inflight_bytes + bytes + r.need > s->cfg.hbm_budget_bytes) {
         evict(s, bytes + r.need, false);
         if (s->resident_bytes + s->inflight_bytes + bytes + r.need > s->cfg.hbm_budget_bytes) {
@@ -293,6 +375,7 @@ void admit(fb_server* s) {
       bt->entries.push_back(e);
       params.push_back(r.params);
       bytes += r.need;
+      cost += cost_of(r.params);
       r.state = State::Running;
       qi = s->queue.erase(qi);
     }
@@ -315,6 +398,8 @@ void admit(fb_server* s) {
     }
     bt->stream_slot = slot;
     bt->bytes = bytes;
+    bt->cost = cost;
+    bt->t_launch = now_ms();
     s->stream_busy[slot] = true;
     s->inflight_bytes += bytes;
     s->inflight.push_back(bt);
