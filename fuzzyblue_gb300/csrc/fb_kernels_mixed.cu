@@ -14,6 +14,8 @@ template __global__ void k_density<true, 0, false>(LaunchArgs);
 template __global__ void k_density<true, 1, false>(LaunchArgs);
 template __global__ void k_density<true, 0, true>(LaunchArgs);
 template __global__ void k_density<true, 1, true>(LaunchArgs);
+template __global__ void k_density<true, 2, false>(LaunchArgs);
+template __global__ void k_density<true, 2, true>(LaunchArgs);
 
 const void* kernel_mixed(int pass, int tpt, int variant, bool order2) {
   const bool v1 = variant == 1;
@@ -21,8 +23,13 @@ const void* kernel_mixed(int pass, int tpt, int variant, bool order2) {
     case kPassTransmittance: return (const void*)k_transmittance<true>;
     case kPassSingle: return (const void*)k_single<true>;
     case kPassDensity:
-      if (order2) return v1 ? (const void*)k_density<true, 1, true> : (const void*)k_density<true, 0, true>;
-      return v1 ? (const void*)k_density<true, 1, false> : (const void*)k_density<true, 0, false>;
+      if (order2)
+        return variant == 2 ? (const void*)k_density<true, 2, true>
+               : v1         ? (const void*)k_density<true, 1, true>
+                            : (const void*)k_density<true, 0, true>;
+      return variant == 2 ? (const void*)k_density<true, 2, false>
+             : v1         ? (const void*)k_density<true, 1, false>
+                          : (const void*)k_density<true, 0, false>;
     case kPassMultiple:
       if (variant == 2) return tpt >= 2 ? (const void*)k_multiple<true, 2, 2> : (const void*)k_multiple<true, 1, 2>;
       return v1 ? (const void*)k_multiple<true, 1, 1> : (const void*)k_multiple<true, 1, 0>;

@@ -15,6 +15,8 @@ template __global__ void k_density<false, 0, false>(LaunchArgs);
 template __global__ void k_density<false, 1, false>(LaunchArgs);
 template __global__ void k_density<false, 0, true>(LaunchArgs);
 template __global__ void k_density<false, 1, true>(LaunchArgs);
+template __global__ void k_density<false, 2, false>(LaunchArgs);
+template __global__ void k_density<false, 2, true>(LaunchArgs);
 
 const void* kernel_plain(int pass, int tpt, int variant, bool order2) {
   const bool v1 = variant == 1;
@@ -22,8 +24,13 @@ const void* kernel_plain(int pass, int tpt, int variant, bool order2) {
     case kPassTransmittance: return (const void*)k_transmittance<false>;
     case kPassSingle: return (const void*)k_single<false>;
     case kPassDensity:
-      if (order2) return v1 ? (const void*)k_density<false, 1, true> : (const void*)k_density<false, 0, true>;
-      return v1 ? (const void*)k_density<false, 1, false> : (const void*)k_density<false, 0, false>;
+      if (order2)
+        return variant == 2 ? (const void*)k_density<false, 2, true>
+               : v1         ? (const void*)k_density<false, 1, true>
+                            : (const void*)k_density<false, 0, true>;
+      return variant == 2 ? (const void*)k_density<false, 2, false>
+             : v1         ? (const void*)k_density<false, 1, false>
+                          : (const void*)k_density<false, 0, false>;
     case kPassMultiple:
       if (variant == 2) return tpt >= 2 ? (const void*)k_multiple<false, 2, 2> : (const void*)k_multiple<false, 1, 2>;
       return v1 ? (const void*)k_multiple<false, 1, 1> : (const void*)k_multiple<false, 1, 0>;

@@ -857,6 +857,19 @@ __device__ __forceinline__ void dens_row(const DensLayout& S, const DensTheta& t
   }
 }
 
+// MIXED density: theta rows summed in FP32 between two Kahan steps.
+constexpr int kDensKahanRows = 2;
+
+// One Kahan step on a (sum, compensation) pair held in shared memory. The
+// pointers are volatile so that the compiler keeps the pair in shared memory
+// rather than forwarding it through registers across theta rows.
+__device__ __forceinline__ void kahan_smem(volatile float* s, volatile float* c, float v) {
+  float sum = *s, comp = *c;
+  Kahan3::add1(sum, comp, v);
+  *s = sum;
+  *c = comp;
+}
+
 template <bool MX, bool TWO>
 __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned char* smem) {
   const int NT = a.dens_n, NNU = a.sc_nu, NK = NNU + 2;
@@ -1025,7 +1038,7 @@ __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned cha
     for (int j = 0; j < kDensMaxGroup; ++j) acc[j] = make_float3(0.f, 0.f, 0.f);
     // (sum, compensation) x 3 x G per thread, element e at accs[e * kDensThreads]:
     // consecutive threads use consecutive banks, offsets are immediates
-    float* accs = S.acc + tid;
+    volatile float* accs = S.acc + tid;
     if (MX) {
 #pragma unroll
       for (int e = 0; e < 6 * kDensMaxGroup; ++e) accs[e * kDensThreads] = 0.f;
@@ -1039,14 +1052,14 @@ __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned cha
         dens_row<TWO, true>(S, t, l, NT, Pl, Ml, mu, mu_s, ox, sx, sy, G, pc, kray, kmie, nu_n1, ir_n1, acc);
       else
         dens_row<TWO, false>(S, t, l, NT, Pl, Ml, mu, mu_s, ox, sx, sy, G, pc, kray, kmie, nu_n1, ir_n1, acc);
-      if (MX) {
-        // Kahan sum over theta rows of the FP32 sums over one row
+      if (MX && ((l + 1) % kDensKahanRows == 0 || l == NT - 1)) {
+        // Kahan sum over theta rows of the FP32 sums over kDensKahanRows rows
 #pragma unroll
         for (int j = 0; j < kDensMaxGroup; ++j) {
           if (j < G) {
-            Kahan3::add1(accs[(6 * j) * kDensThreads], accs[(6 * j + 3) * kDensThreads], acc[j].x);
-            Kahan3::add1(accs[(6 * j + 1) * kDensThreads], accs[(6 * j + 4) * kDensThreads], acc[j].y);
-            Kahan3::add1(accs[(6 * j + 2) * kDensThreads], accs[(6 * j + 5) * kDensThreads], acc[j].z);
+            kahan_smem(accs + (6 * j) * kDensThreads, accs + (6 * j + 3) * kDensThreads, acc[j].x);
+            kahan_smem(accs + (6 * j + 1) * kDensThreads, accs + (6 * j + 4) * kDensThreads, acc[j].y);
+            kahan_smem(accs + (6 * j + 2) * kDensThreads, accs + (6 * j + 5) * kDensThreads, acc[j].z);
             acc[j] = make_float3(0.f, 0.f, 0.f);
           }
         }
@@ -1218,10 +1231,11 @@ __device__ void tile_indirect(const DevAtmo& a, int order, int tile, unsigned ch
 }
 
 // V selects the occupancy variant chosen by the autotuner: V = 0 caps the
-// registers for 4 resident blocks per SM, V = 1 for 3. TWO: the launch of
-// order 2, whose lookups read the single-scattering Rayleigh and Mie tables.
+// registers for 4 resident blocks per SM, V = 1 for 3, V = 2 for 5. TWO: the
+// launch of order 2, whose lookups read the single-scattering Rayleigh and
+// Mie tables.
 template <bool MX, int V, bool TWO>
-__global__ void __launch_bounds__(kDensThreads, V == 0 ? 4 : 3) k_density(LaunchArgs L) {
+__global__ void __launch_bounds__(kDensThreads, V == 0 ? 4 : (V == 1 ? 3 : 5)) k_density(LaunchArgs L) {
   extern __shared__ __align__(16) unsigned char smem[];
   int seg, job, tile;
   int taken = 0;

@@ -282,7 +282,7 @@ int fb_batch_build(fb_builder* b, void* stream, const fb_params* params,
 typedef struct fb_tile_shape {
     uint32_t density_columns;  /* mu_s columns per scattering-density tile */
     uint32_t density_rows;     /* mu rows per scattering-density tile */
-    uint32_t density_variant;  /* occupancy variant of the density kernel (0, 1) */
+    uint32_t density_variant;  /* density kernel occupancy: 0, 1, 2 = 4, 3, 5 blocks per SM */
     uint32_t multiple_variant; /* occupancy variant of the multiple-scattering kernel */
     float density_ms;          /* measured time of the chosen density launch */
     float multiple_ms;         /* measured time of the chosen multiple-scattering launch */
