@@ -149,6 +149,14 @@ namespace fbi {
 
 // Geometry tables (order-independent, written by the first two launches):
 // rows, x columns, multiple-scattering sample records, density r / theta records.
+// Indirect-irradiance records of the mixed mode.
+size_t irgeo_bytes(const fb_params& p) {
+  const fb_params_raw& r = p.raw;
+  const size_t ir_r = r.irradiance_r_size, ir_mus = r.irradiance_mu_s_size;
+  return align256(sizeof(fb::IrZ) * ir_r) + align256(sizeof(fb::Axis) * ir_r * (p.irradiance_samples / 2)) +
+         align256(sizeof(fb::Axis) * ir_mus * (r.scattering_nu_size + 2)) + align256(sizeof(float) * ir_mus);
+}
+
 size_t geometry_bytes(const fb_params& p) {
   const fb_params_raw& r = p.raw;
   const size_t rows = (size_t)r.scattering_mu_size * r.scattering_r_size;
@@ -156,16 +164,26 @@ size_t geometry_bytes(const fb_params& p) {
   return align256(sizeof(fb::RowGeo) * rows) + align256(sizeof(fb::ColGeo) * W) +
          align256(sizeof(fb::MSRec) * rows * (p.multiple_scattering_steps + 1)) +
          align256(sizeof(fb::DensZ) * r.scattering_r_size) +
-         align256(sizeof(fb::ThetaRec) * r.scattering_r_size * p.density_samples);
+         align256(sizeof(fb::ThetaRec) * r.scattering_r_size * p.density_samples) +
+         (p.precision == FB_PRECISION_MIXED ? irgeo_bytes(p) : 0);
 }
 
-void place_geometry(fb::DevAtmo& d, char*& tp) {
+void place_geometry(fb::DevAtmo& d, char*& tp, bool mixed) {
   const size_t rows = (size_t)d.sc_mu * d.sc_r;
   d.g_rows = (fb::RowGeo*)tp;   tp += align256(sizeof(fb::RowGeo) * rows);
   d.g_cols = (fb::ColGeo*)tp;   tp += align256(sizeof(fb::ColGeo) * (size_t)d.W);
   d.g_ms = (fb::MSRec*)tp;      tp += align256(sizeof(fb::MSRec) * rows * (d.ms_steps + 1));
   d.g_z = (fb::DensZ*)tp;       tp += align256(sizeof(fb::DensZ) * (size_t)d.sc_r);
   d.g_th = (fb::ThetaRec*)tp;   tp += align256(sizeof(fb::ThetaRec) * (size_t)d.sc_r * d.dens_n);
+  d.g_irz = nullptr;
+  d.g_iry = d.g_irx = nullptr;
+  d.g_irmus = nullptr;
+  if (mixed) {
+    d.g_irz = (fb::IrZ*)tp;   tp += align256(sizeof(fb::IrZ) * (size_t)d.ir_r);
+    d.g_iry = (fb::Axis*)tp;  tp += align256(sizeof(fb::Axis) * (size_t)d.ir_r * (d.irr_n / 2));
+    d.g_irx = (fb::Axis*)tp;  tp += align256(sizeof(fb::Axis) * (size_t)d.ir_mus * (d.sc_nu + 2));
+    d.g_irmus = (float*)tp;   tp += align256(sizeof(float) * (size_t)d.ir_mus);
+  }
 }
 
 TableSizes sizes_of(const fb_params& p) {
@@ -524,7 +542,8 @@ void plan_group(Plan& P, const std::vector<DevAtmo>& A, const std::vector<int>& 
     std::vector<int> tiles, tg;
     for (int j : group) {
       tiles.push_back(fb::tiles_transmittance(A[j].tr_mu, A[j].tr_r));
-      tg.push_back(fb::tiles_geometry(A[j].W, A[j].sc_mu, A[j].sc_r));
+      tg.push_back(fb::tiles_geometry(
+          A[j].W, A[j].sc_mu, A[j].sc_r, mixed ? fb::irgeo_entries(A[j].ir_r, A[j].ir_mus, A[j].irr_n, A[j].sc_nu) : 0));
       L.texels += (uint64_t)A[j].tr_mu * A[j].tr_r;
     }
     add_segment(P, L, 0, group, tiles);
@@ -721,7 +740,7 @@ int build(fb_builder* b, cudaStream_t s, const fb_params* params, uint32_t count
       d.sc_acc = (double*)tp; tp += align256(24 * z.nsc);
       d.ir_acc = (double*)tp; tp += align256(24 * z.nir);
     }
-    place_geometry(d, tp);
+    place_geometry(d, tp, params[i].precision == FB_PRECISION_MIXED);
   }
   // work plan
   Plan plan;

@@ -72,6 +72,15 @@ struct ThetaRec {
   int pad;
 };
 
+// Indirect irradiance, MIXED (indirect_irradiance.comp:16-40 lookups): per
+// irradiance r row the radius and the r axis of the 3D tables; the mu axes per
+// (r row, theta row) and the x axes per (mu_s column, nu slice -1 .. nu_size)
+// are separate arrays.
+struct IrZ {
+  float r;
+  Axis az;
+};
+
 // One atmosphere as the kernels see it: parameters (ParamsRaw fields,
 // src/precompute.rs:937-964), sizes, sample counts and its tables.
 struct DevAtmo {
@@ -108,6 +117,10 @@ struct DevAtmo {
   MSRec* g_ms;      // sc_mu * sc_r * (ms_steps + 1)
   DensZ* g_z;       // sc_r
   ThetaRec* g_th;   // sc_r * dens_n
+  IrZ* g_irz;       // MIXED: ir_r
+  Axis* g_iry;      // MIXED: ir_r * irr_n / 2
+  Axis* g_irx;      // MIXED: ir_mus * (sc_nu + 2)
+  float* g_irmus;   // MIXED: ir_mus
 };
 
 constexpr float kPiF = 3.14159265358979323846f;
@@ -173,6 +186,14 @@ __device__ __forceinline__ Axis make_axis(float coord, int n) {
   int i = (int)fl;
   a.i0 = min(max(i, 0), n - 1);
   a.i1 = min(max(i + 1, 0), n - 1);
+  return a;
+}
+
+// An axis read back from a geometry record, its indices bounded to [0, n - 1]
+// so that a damaged record cannot address outside its table.
+__device__ __forceinline__ Axis bounded_axis(Axis a, int n) {
+  a.i0 = min(max(a.i0, 0), n - 1);
+  a.i1 = min(max(a.i1, 0), n - 1);
   return a;
 }
 

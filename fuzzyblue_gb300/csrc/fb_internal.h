@@ -74,6 +74,6 @@ namespace fbi {
 void fill_atmo_record(fb::DevAtmo& d, const fb_params& p);
 // Points the record's geometry tables at `tp` and advances it past them
 // (the last part of the temporaries, sizes_of(p).tmp_bytes counts them).
-void place_geometry(fb::DevAtmo& d, char*& tp);
+void place_geometry(fb::DevAtmo& d, char*& tp, bool mixed);
 
 }  // namespace fbi

@@ -156,7 +156,7 @@ extern "C" int fb_atmosphere_build_noalloc(void* stream, const fb_params* p, voi
   }
   {
     char* gp = (char*)tp;
-    fbi::place_geometry(d, gp);
+    fbi::place_geometry(d, gp, mixed);
   }
   // launches of the pass order (src/precompute.rs:1726-1999), one job each
   std::vector<int> ints(n_ints, 0);  // job ids 0, offsets 0
@@ -187,7 +187,9 @@ extern "C" int fb_atmosphere_build_noalloc(void* stream, const fb_params* p, voi
   };
   const bool multi = d.order >= 2;
   add(fb::kPassTransmittance, 0,
-      {fb::tiles_transmittance(d.tr_mu, d.tr_r), fb::tiles_geometry(d.W, d.sc_mu, d.sc_r)}, 0, 1, fb::kThreads, 0);
+      {fb::tiles_transmittance(d.tr_mu, d.tr_r),
+       fb::tiles_geometry(d.W, d.sc_mu, d.sc_r, mixed ? fb::irgeo_entries(d.ir_r, d.ir_mus, d.irr_n, d.sc_nu) : 0)},
+      0, 1, fb::kThreads, 0);
   add(fb::kPassSingle, 0,
       {fb::tiles_rows(d.W, d.sc_mu, d.sc_r), fb::tiles_direct(d.ir_mus, d.ir_r),
        multi ? fb::tiles_msrec(d.sc_mu, d.sc_r, d.ms_steps) : 0, multi ? fb::tiles_densgeo(d.sc_r, d.dens_n) : 0},

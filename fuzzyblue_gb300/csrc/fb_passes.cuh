@@ -16,6 +16,7 @@
 // atmosphere, located by binary search over per-atmosphere item offsets.
 #pragma once
 
+#include <cstddef>
 #include "fb_device.cuh"
 
 namespace fb {
@@ -232,6 +233,45 @@ template <bool MX> __device__ void tile_direct(const DevAtmo& a, int tile) {
 // 1): one thread per x column (ColGeo: mu_s and raw nu) and per (mu, r) row
 // (RowGeo: the view ray). PLAIN values are the reference's float decode
 // (scattering.h:62-137), MIXED values its FP64 form.
+// Entry q of the indirect-irradiance records (MIXED; the FP64 decodes of
+// indirect_irradiance.comp:16-40 that do not depend on the order).
+__device__ inline void tile_irgeo(const DevAtmo& a, int q) {
+  const int NT = a.irr_n / 2, NK = a.sc_nu + 2;
+  Geo64 G;
+  G.init(a);
+  auto row_q = [&](int j) {
+    const double h = (double(j) / double(a.ir_r - 1)) * (G.T - G.R), rd = G.R + h;
+    return h * (rd + G.R);
+  };
+  auto col_mus = [&](int i) { return clamp_cosine(2.0 * (double(i) / double(a.ir_mus - 1)) - 1.0); };
+  if (q < a.ir_r) {
+    const int j = q;
+    const double h = (double(j) / double(a.ir_r - 1)) * (G.T - G.R);
+    IrZ o;
+    o.r = (float)(G.R + h);
+    o.az = axis_texel(G.sc_r_texel(a, row_q(j)), a.sc_r);
+    a.g_irz[j] = o;
+    return;
+  }
+  q -= a.ir_r;
+  if (q < a.ir_r * NT) {
+    const int j = q / NT, l = q % NT;
+    const double qd = row_q(j);
+    const double ct = cos((double(l) + 0.5) * (kPiD / double(a.irr_n)));
+    a.g_iry[q] = axis_texel(G.sc_mu_texel(a, qd, G.radius(qd) * ct, false), a.sc_mu);
+    return;
+  }
+  q -= a.ir_r * NT;
+  if (q < a.ir_mus * NK) {
+    const int i = q / NK, s = q % NK;
+    const double ymus = G.mus_unit(a, col_mus(i));
+    a.g_irx[q] = axis_texel(double(s - 1) * a.sc_mus + ymus * double(a.sc_mus - 1), a.W);
+    return;
+  }
+  q -= a.ir_mus * NK;
+  if (q < a.ir_mus) a.g_irmus[q] = (float)col_mus(q);
+}
+
 template <bool MX> __device__ void tile_geometry(const DevAtmo& a, int tile) {
   const int k = tile * kThreads + threadIdx.x;
   const int nrows = a.sc_mu * a.sc_r;
@@ -292,11 +332,20 @@ template <bool MX> __device__ void tile_geometry(const DevAtmo& a, int tile) {
       o.rr = o.two_r_mu = o.r_mu = 0.f;
     }
     a.g_rows[row] = o;
+  } else if (MX) {
+    tile_irgeo(a, k - a.W - nrows);
   }
 }
 
-__host__ __device__ inline int tiles_geometry(int W, int sc_mu, int sc_r) {
-  return (W + sc_mu * sc_r + kThreads - 1) / kThreads;
+// Entries of the indirect-irradiance records (MIXED), in the order tile_irgeo
+// fills them.
+__host__ __device__ inline int irgeo_entries(int ir_r, int ir_mus, int irr_n, int sc_nu) {
+  return ir_r + ir_r * (irr_n / 2) + ir_mus * (sc_nu + 2) + ir_mus;
+}
+// Geometry work items of one atmosphere: x columns and (mu, r) rows, then in
+// the mixed mode the indirect-irradiance records.
+__host__ __device__ inline int tiles_geometry(int W, int sc_mu, int sc_r, int ir_entries) {
+  return (W + sc_mu * sc_r + ir_entries + kThreads - 1) / kThreads;
 }
 
 template <bool MX> __global__ void __launch_bounds__(kThreads) k_transmittance(LaunchArgs L) {
@@ -886,13 +935,13 @@ __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned cha
   // geometry tables
   const DensZ zr = a.g_z[zi];
   const float r = zr.r;
-  const Axis s_az = zr.az, s_irx = zr.irx;
+  const Axis s_az = bounded_axis(zr.az, a.sc_r), s_irx = bounded_axis(zr.irx, a.ir_r);
   const ThetaRec* thr = a.g_th + (size_t)zi * NT;
   for (int k = tid; k < NT + ns + (MX ? ny + NNU : 0); k += nth) {
     if (k < NT) {
       const ThetaRec t = thr[k];
       S.th[k] = t.th;
-      S.tay[k] = t.tay;
+      S.tay[k] = bounded_axis(t.tay, a.sc_mu);
     } else if (k < NT + ns) {
       const int c = k - NT, si = s0 + c;
       const ColGeo cg = a.g_cols[si];
@@ -1103,7 +1152,6 @@ __device__ void tile_indirect(const DevAtmo& a, int order, int tile, unsigned ch
   const int i = t % a.ir_mus, j = t / a.ir_mus;
   float r, mu_s, u_ms = 0.f;
   Axis az;
-  double qd = 0.0, ymus = 0.0;
   if (!MX) {
     Geo32 G;
     G.init(a);
@@ -1113,16 +1161,11 @@ __device__ void tile_indirect(const DevAtmo& a, int order, int tile, unsigned ch
     az = make_axis(G.u_r(a, r), a.sc_r);
     u_ms = G.u_mu_s(a, mu_s);
   } else {
-    Geo64 G;
-    G.init(a);
-    const double x_mu_s = double(i) / double(a.ir_mus - 1), x_r = double(j) / double(a.ir_r - 1);
-    const double h = x_r * (G.T - G.R), rd = G.R + h;
-    qd = h * (rd + G.R);
-    r = (float)rd;
-    const double mus = clamp_cosine(2.0 * x_mu_s - 1.0);
-    mu_s = (float)mus;
-    az = axis_texel(G.sc_r_texel(a, qd), a.sc_r);
-    ymus = G.mus_unit(a, mus);
+    // the FP64 decodes come from the records of the build (tile_irgeo)
+    const IrZ z = a.g_irz[j];
+    r = z.r;
+    az = bounded_axis(z.az, a.sc_r);
+    mu_s = a.g_irmus[i];
   }
   const float4* src0 = one ? a.dr : a.dms;
   const float dthetaf = kPiF / float(a.irr_n), dphif = kPiF / float(a.irr_n);
@@ -1137,11 +1180,8 @@ __device__ void tile_indirect(const DevAtmo& a, int order, int tile, unsigned ch
       ay = make_axis(G.u_mu(a, r, ct, false), a.sc_mu);
       ax = make_axis((float(s - 1) + u_ms) / float(NNU), a.W);
     } else {
-      Geo64 G;
-      G.init(a);
-      const double ct = cos((double(l) + 0.5) * (kPiD / double(a.irr_n)));
-      ay = axis_texel(G.sc_mu_texel(a, qd, G.radius(qd) * ct, false), a.sc_mu);
-      ax = axis_texel(double(s - 1) * a.sc_mus + ymus * double(a.sc_mus - 1), a.W);
+      ay = bounded_axis(a.g_iry[j * NT + l], a.sc_mu);
+      ax = bounded_axis(a.g_irx[i * NK + s], a.W);
     }
     const float3 v = fetch3(src0, a.W, a.sc_mu, ax, ay, az);
     P[k] = make_float4(v.x, v.y, v.z, 0.f);
@@ -1320,11 +1360,26 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
     const int b = k / (nrow * ng), rem = k % (nrow * ng);
     slab[b * slab_stride + (rem / ng) * SR + W + rem % ng] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
-  {  // this tile's sample records
+  {  // this tile's sample records, their (mu, r) indices bounded to the table
+    static_assert(sizeof(MSRec) == 3 * sizeof(int4), "MSRec is three 16-byte words");
+    static_assert(offsetof(MSRec, y0) == 28 && offsetof(MSRec, y1) == 32 && offsetof(MSRec, z0) == 36 &&
+                      offsetof(MSRec, z1) == 40,
+                  "MSRec index words");
     const int4* src = reinterpret_cast<const int4*>(a.g_ms + (size_t)row0 * NS);
     int4* dst = reinterpret_cast<int4*>(rec);
-    const int n16 = nrow * NS * (int)(sizeof(MSRec) / sizeof(int4));
-    for (int k = tid; k < n16; k += nth) dst[k] = __ldg(src + k);
+    const int ymax = a.sc_mu - 1, zmax = a.sc_r - 1;
+    for (int k = tid; k < nrow * NS; k += nth) {
+      const int4 w0 = __ldg(src + 3 * k);
+      int4 w1 = __ldg(src + 3 * k + 1), w2 = __ldg(src + 3 * k + 2);
+      // words 7..10: y0, y1, z0, z1
+      w1.w = min(max(w1.w, 0), ymax);
+      w2.x = min(max(w2.x, 0), ymax);
+      w2.y = min(max(w2.y, 0), zmax);
+      w2.z = min(max(w2.z, 0), zmax);
+      dst[3 * k] = w0;
+      dst[3 * k + 1] = w1;
+      dst[3 * k + 2] = w2;
+    }
   }
   // per-texel constants (TPT texels per thread): row, slab entry, texel x
   float c_rmus[TPT], c_nu[TPT], c_lerp[TPT];
