@@ -307,8 +307,9 @@ extern "C" int fb_builder_create(int device, fb_builder** out) {
   for (int mode = 0; mode < 2; ++mode)
     for (int pass = 0; pass < 4; ++pass)
       for (int tpt : {1, 2})
-        for (int variant : {0, 1, 2, 3, 4, 5}) {
-        const void* k = fb::kernel_for(mode == 1, pass, tpt, variant % 3, variant >= 3);
+        for (int variant = 0; variant < 12; ++variant) {
+        // variants 0..5 (density: occupancy + clamped tables), of order 2 or not
+        const void* k = fb::kernel_for(mode == 1, pass, tpt, variant % 6, variant >= 6);
         cudaFuncAttributes kfa;
         if (cudaFuncGetAttributes(&kfa, k) != cudaSuccess ||
             cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -522,8 +523,10 @@ int launch_variant(const std::vector<DevAtmo>& A, const std::vector<int>& jobs, 
   return e ? (density ? e->dens_variant : e->ms_variant) : 0;
 }
 
+// smem_limit: dynamic shared memory a launch may use; density launches whose
+// power-of-two interval tables would exceed it use the clamped tables.
 void plan_group(Plan& P, const std::vector<DevAtmo>& A, const std::vector<int>& group, bool mixed,
-                const fbi::Tuning& tun) {
+                const fbi::Tuning& tun, size_t smem_limit) {
   if (group.empty()) return;
   int max_order = 1;
   for (int j : group) max_order = std::max(max_order, A[j].order);
@@ -579,18 +582,20 @@ void plan_group(Plan& P, const std::vector<DevAtmo>& A, const std::vector<int>& 
       if (A[j].order >= n) jobs.push_back(j);
     PlannedLaunch D = mk(fb::kPassDensity, n);
     std::vector<int> t0, t1;
+    bool cl = false;
+    for (int j : jobs) cl |= fb::density_smem(A[j], n == 2, mixed, false) > smem_limit;
     for (int j : jobs) {
       const DevAtmo& a = A[j];
       t0.push_back(fb::tiles_density(a));
       t1.push_back(fb::tiles_indirect(a.ir_mus, a.ir_r));
-      D.smem = std::max(D.smem, fb::density_smem(a, n == 2, mixed));
+      D.smem = std::max(D.smem, fb::density_smem(a, n == 2, mixed, cl));
       D.smem = std::max(D.smem, fb::indirect_smem(a.irr_n, a.sc_nu, n - 1 == 1));
       D.texels += (uint64_t)a.W * a.sc_mu * a.sc_r + (uint64_t)a.ir_mus * a.ir_r;
     }
     add_segment(P, D, 0, jobs, t0);
     add_segment(P, D, 1, jobs, t1);
     D.nseg = 2;
-    D.variant = launch_variant(A, jobs, tun, mixed, true);
+    D.variant = launch_variant(A, jobs, tun, mixed, true) + (cl ? fb::kDensClamped : 0);
     P.launches.push_back(D);
     PlannedLaunch M = mk(fb::kPassMultiple, n);
     std::vector<int> tm;
@@ -746,8 +751,9 @@ int build(fb_builder* b, cudaStream_t s, const fb_params* params, uint32_t count
   Plan plan;
   std::vector<int> g_plain, g_mixed;
   for (uint32_t i = 0; i < count; ++i) (params[i].precision == FB_PRECISION_MIXED ? g_mixed : g_plain).push_back((int)i);
-  plan_group(plan, P->dev, g_plain, false, tun);
-  plan_group(plan, P->dev, g_mixed, true, tun);
+  const size_t smem_limit = (size_t)std::max(0, b->smem_optin - 1024);
+  plan_group(plan, P->dev, g_plain, false, tun, smem_limit);
+  plan_group(plan, P->dev, g_mixed, true, tun, smem_limit);
   const size_t atm_bytes = align256(sizeof(DevAtmo) * count);
   const size_t int_bytes = align256(sizeof(int) * std::max<size_t>(plan.ints.size(), 1));
   const size_t cnt_bytes = align256(sizeof(unsigned) * plan.launches.size());

@@ -10,26 +10,39 @@ template __global__ void k_multiple<true, 1, 0>(LaunchArgs);
 template __global__ void k_multiple<true, 1, 1>(LaunchArgs);
 template __global__ void k_multiple<true, 1, 2>(LaunchArgs);
 template __global__ void k_multiple<true, 2, 2>(LaunchArgs);
-template __global__ void k_density<true, 0, false>(LaunchArgs);
-template __global__ void k_density<true, 1, false>(LaunchArgs);
-template __global__ void k_density<true, 0, true>(LaunchArgs);
-template __global__ void k_density<true, 1, true>(LaunchArgs);
-template __global__ void k_density<true, 2, false>(LaunchArgs);
-template __global__ void k_density<true, 2, true>(LaunchArgs);
+
+template __global__ void k_density<true, 0, false, false>(LaunchArgs);
+template __global__ void k_density<true, 1, false, false>(LaunchArgs);
+template __global__ void k_density<true, 2, false, false>(LaunchArgs);
+template __global__ void k_density<true, 0, true, false>(LaunchArgs);
+template __global__ void k_density<true, 1, true, false>(LaunchArgs);
+template __global__ void k_density<true, 2, true, false>(LaunchArgs);
+template __global__ void k_density<true, 0, false, true>(LaunchArgs);
+template __global__ void k_density<true, 1, false, true>(LaunchArgs);
+template __global__ void k_density<true, 2, false, true>(LaunchArgs);
+template __global__ void k_density<true, 0, true, true>(LaunchArgs);
+template __global__ void k_density<true, 1, true, true>(LaunchArgs);
+template __global__ void k_density<true, 2, true, true>(LaunchArgs);
 
 const void* kernel_mixed(int pass, int tpt, int variant, bool order2) {
   const bool v1 = variant == 1;
   switch (pass) {
     case kPassTransmittance: return (const void*)k_transmittance<true>;
     case kPassSingle: return (const void*)k_single<true>;
-    case kPassDensity:
-      if (order2)
-        return variant == 2 ? (const void*)k_density<true, 2, true>
-               : v1         ? (const void*)k_density<true, 1, true>
-                            : (const void*)k_density<true, 0, true>;
-      return variant == 2 ? (const void*)k_density<true, 2, false>
-             : v1         ? (const void*)k_density<true, 1, false>
-                          : (const void*)k_density<true, 0, false>;
+    case kPassDensity: {
+      // variant: occupancy variant (0..2) + kDensClamped for clamped tables
+      static const void* const k[2][2][3] = {
+          {{(const void*)k_density<true, 0, false, false>, (const void*)k_density<true, 1, false, false>,
+            (const void*)k_density<true, 2, false, false>},
+           {(const void*)k_density<true, 0, true, false>, (const void*)k_density<true, 1, true, false>,
+            (const void*)k_density<true, 2, true, false>}},
+          {{(const void*)k_density<true, 0, false, true>, (const void*)k_density<true, 1, false, true>,
+            (const void*)k_density<true, 2, false, true>},
+           {(const void*)k_density<true, 0, true, true>, (const void*)k_density<true, 1, true, true>,
+            (const void*)k_density<true, 2, true, true>}}};
+      const int v = variant < 0 ? 0 : variant;
+      return k[v >= kDensClamped ? 1 : 0][order2 ? 1 : 0][(v % kDensClamped) % 3];
+    }
     case kPassMultiple:
       if (variant == 2) return tpt >= 2 ? (const void*)k_multiple<true, 2, 2> : (const void*)k_multiple<true, 1, 2>;
       return v1 ? (const void*)k_multiple<true, 1, 1> : (const void*)k_multiple<true, 1, 0>;

@@ -70,8 +70,9 @@ int setup_device(int dev, DeviceSetup** out) {
     for (int mode = 0; mode < 2; ++mode)
       for (int pass = 0; pass < 4; ++pass)
         for (int tpt : {1, 2})
-          for (int variant : {0, 2, 3}) {
-          const void* k = fb::kernel_for(mode == 1, pass, tpt, variant == 2 ? 2 : 0, variant == 3);
+          for (int variant : {0, 2, fb::kDensClamped, 10, 12, 10 + fb::kDensClamped}) {
+          // variants 0, 2 and clamped density tables, of order 2 (+ 10) or not
+          const void* k = fb::kernel_for(mode == 1, pass, tpt, variant % 10, variant >= 10);
           cudaFuncAttributes fa;
           if (cudaFuncGetAttributes(&fa, k) != cudaSuccess ||
               cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -196,8 +197,10 @@ extern "C" int fb_atmosphere_build_noalloc(void* stream, const fb_params* p, voi
       fb::ss_smem(d.W, d.ss_steps, d.sc_mus, d.sc_nu), 1, fb::kThreads, 0);
   const int ms_block = fb::ms_threads(d.W);
   for (int n = 2; n <= d.order; ++n) {
-    const size_t sm = std::max(fb::density_smem(d, n == 2, mixed), fb::indirect_smem(d.irr_n, d.sc_nu, n - 1 == 1));
-    add(fb::kPassDensity, n, {fb::tiles_density(d), fb::tiles_indirect(d.ir_mus, d.ir_r)}, sm, 1, fb::kDensThreads, 0);
+    const bool cl = fb::density_smem(d, n == 2, mixed, false) > (size_t)std::max(0, ds->smem_optin - 1024);
+    const size_t sm = std::max(fb::density_smem(d, n == 2, mixed, cl), fb::indirect_smem(d.irr_n, d.sc_nu, n - 1 == 1));
+    add(fb::kPassDensity, n, {fb::tiles_density(d), fb::tiles_indirect(d.ir_mus, d.ir_r)}, sm, 1, fb::kDensThreads,
+        cl ? fb::kDensClamped : 0);
     add(fb::kPassMultiple, n, {fb::tiles_multiple(d.W, d.sc_mus, d.ms_steps, d.sc_mu, d.sc_r, ms_block)},
         fb::ms_smem(d.W, d.ms_steps, d.sc_mus, ms_block), fb::ms_shape(d.W, d.sc_mus, d.ms_steps, ms_block).TPT, ms_block,
         ms_block > fb::kThreads ? 2 : 0);

@@ -756,23 +756,47 @@ __host__ __device__ inline DensShape dens_shape(int sc_r, int sc_mu, int sc_mus,
   return d;
 }
 
-// An entry of a linearly interpolated RGB table: value in a.xyz, difference to
-// the next entry in (a.w, b.x, b.y); 32 bytes, read as one 16- and one 8-byte
-// load from the same base address.
+// One interval [k, k + 1] of a linearly interpolated RGB table: the value at
+// its midpoint k + 1/2 in a.xyz, the difference of its two entries in
+// (a.w, b.x, b.y); 32 bytes, read as one 16- and one 8-byte load from the same
+// base address. The value at position t in the interval is
+// a.xyz + (t - k - 1/2) (a.w, b.x, b.y).
 struct LerpRec {
   float4 a;
   float2 b;
   float2 pad;
 };
 
+// The density tile's interval tables have a power-of-two number of records,
+// addressed by k & (size - 1): intervals k >= 0 at position k, the interval
+// k = -1 (below the first entry) at the last position, so that any k, even
+// one derived from a NaN, stays inside the table. Where such tables do not
+// fit in shared memory (CL: the largest nu and irradiance sizes), they hold
+// exactly the intervals, k at position k + 1, and the position is clamped.
+__host__ __device__ inline int pow2_at_least(int n) {
+  int p = 1;
+  while (p < n) p <<= 1;
+  return p;
+}
+// nu intervals -1 .. nu_size of the reduced table (slices -1 .. nu_size + 1)
+__host__ __device__ inline int dens_mk(int sc_nu, bool cl) { return cl ? sc_nu + 2 : pow2_at_least(sc_nu + 2); }
+// ground irradiance intervals -1 .. ir_mus - 1
+__host__ __device__ inline int dens_mke(int ir_mus, bool cl) { return cl ? ir_mus + 1 : pow2_at_least(ir_mus + 1); }
+// Position of interval k in a table of n records, and the interval at position p.
+template <bool CL> __device__ __forceinline__ int rec_pos(int k, int n) { return CL ? k + 1 : (k & (n - 1)); }
+template <bool CL> __device__ __forceinline__ int rec_interval(int p, int n) {
+  return CL ? p - 1 : (p == n - 1 ? -1 : p);
+}
+
 struct DensLayout {
   DensTheta* th;    // NT
   Axis* tay;        // NT: theta -> mu axis
   Axis* kax;        // S * NK: (column, nu slice) -> x axis
-  float4* dir;      // NT * NT mirror pairs: (cos phi sin t, sin phi sin t, ground normal x, y)
-  float* gnz;       // NT * NT: ground normal z
-  LerpRec* P;       // per table, S * NT * NK: value rgb and delta to the next nu slice
-  LerpRec* E;       // ir_mus: ground irradiance row (the two sampler rows pre-blended) and delta
+  float4* dir;      // NT * NT mirror pairs: (cos phi sin t, sin phi sin t) x (nu_size - 1) / 2,
+                    // (ground normal x, y) x (ir_mus - 1) / 2
+  float* gnz;       // NT * NT: ground normal z x (ir_mus - 1) / 2
+  LerpRec* P;       // per table, S * NT * MK: nu intervals of the previous order (dens_mk)
+  LerpRec* E;       // MKE: intervals of the ground irradiance row, the two sampler rows pre-blended (dens_mke)
   float* col_mus;   // S
   double* col_musd; // S (MIXED)
   double2* ymu;     // chunk (MIXED): (mu, 1 - mu^2)
@@ -781,9 +805,9 @@ struct DensLayout {
 };
 
 __host__ __device__ inline size_t dens_layout(unsigned char* base, int dens_n, int sc_nu, int ir_mus, int S,
-                                              int chunk, bool two, bool mixed, DensLayout* L) {
+                                              int chunk, bool two, bool mixed, bool cl, DensLayout* L) {
   const int NT = dens_n, NK = sc_nu + 2;
-  const size_t nP = (size_t)S * NT * NK * (two ? 2 : 1);
+  const size_t nP = (size_t)S * NT * dens_mk(sc_nu, cl) * (two ? 2 : 1);
   size_t o = 0;
   auto take = [&](size_t bytes) {
     size_t at = o;
@@ -792,7 +816,7 @@ __host__ __device__ inline size_t dens_layout(unsigned char* base, int dens_n, i
   };
   size_t o_th = take(sizeof(DensTheta) * NT), o_tay = take(sizeof(Axis) * NT), o_kax = take(sizeof(Axis) * S * NK);
   size_t o_dir = take(sizeof(float4) * NT * NT), o_gnz = take(sizeof(float) * NT * NT);
-  size_t o_P = take(sizeof(LerpRec) * nP), o_E = take(sizeof(LerpRec) * ir_mus);
+  size_t o_P = take(sizeof(LerpRec) * nP), o_E = take(sizeof(LerpRec) * dens_mke(ir_mus, cl));
   size_t o_cm = take(sizeof(float) * S), o_cmd = take(sizeof(double) * S);
   size_t o_ymu = take(mixed ? sizeof(double2) * chunk : 0), o_nu = take(mixed ? sizeof(double) * sc_nu : 0);
   size_t o_acc = take(mixed ? sizeof(float) * kDensThreads * kDensMaxGroup * 6 : 0);
@@ -827,42 +851,56 @@ struct PhaseCoef {
   }
 };
 
-// Linear interpolation position in a table of n entries for a cosine c in
-// [-1, 1] (texel coordinate (c + 1) / 2 (n - 1), the sampler's u n - 1/2 for
-// u = coord_from_unit((c + 1) / 2)): entry k in [0, n - 2] and weight f in
-// [0, 1] of entry k + 1. Rounding (t - 1/2) to an integer through the float
-// adder (adding 1.5 * 2^23) gives floor(t), or floor(t) - 1 with f = 1 where t
-// is an integer: the same interpolated value. The saturation clamps rounding
-// excursions of c beyond [-1, 1], so k never leaves the table.
+// Interval of a table position. For a cosine c in [-1, 1] the linear texel
+// coordinate is t = (c + 1) / 2 (n - 1) in a table of n entries (the
+// sampler's u n - 1/2 for u = coord_from_unit((c + 1) / 2)); the callers form
+// w = t - 1/2 directly, with the scale folded into their direction tables.
+// Rounding w to an integer k through the float adder (adding 1.5 * 2^23) gives
+// the interval [k, k + 1] that holds t (or, where t is an integer, the
+// neighbouring one: the same value), fr = w - k in [-1/2, 1/2] its offset from
+// the interval's midpoint, and the record position in a table of n records:
+// k & (n - 1) (the float's low bits; 1.5 * 2^23 has none set), or for CL
+// k + 1 clamped to [0, n - 1] (negative values wrap to large unsigned ones).
+// Rounding excursions of c just beyond [-1, 1] give k = -1 or k = n - 1,
+// whose records extrapolate by the excursion.
 constexpr float kRoundMagic = 12582912.0f;  // 1.5 * 2^23
 constexpr int kRoundMagicBits = 0x4B400000;
-__device__ __forceinline__ int lerp_pos(float c, float n_minus_1, float& f) {
-  const float u = __saturatef(fmaf(c, 0.5f, 0.5f));
-  const float y = fmaf(u, n_minus_1, -0.5f) + kRoundMagic;
-  f = fmaf(u, n_minus_1, -(y - kRoundMagic));
-  return __float_as_int(y) - kRoundMagicBits;
+template <bool CL> __device__ __forceinline__ int mid_pos(float w, int n, float& fr) {
+  const float y = w + kRoundMagic;
+  fr = w - (y - kRoundMagic);
+  if (CL) return (int)min((unsigned)(__float_as_int(y) - (kRoundMagicBits - 1)), (unsigned)(n - 1));
+  return __float_as_int(y) & (n - 1);
 }
 
 // The directions of one theta row for the G texels of a thread (all sharing
 // r, mu and mu_s): incident radiance of order n - 1 from the reduced table
 // (scattering.h:139-179), plus for rows that meet the ground the ground
 // bounce (scattering_density.comp:64-84), times the phase functions
-// (scattering_density.comp:86-104).
-template <bool TWO, bool GROUND>
+// (scattering_density.comp:86-104). Table positions come as w = t - 1/2
+// (mid_pos): the direction table holds cos phi sin t and sin phi sin t scaled
+// by (nu_size - 1) / 2 and the ground normal scaled by (ir_mus - 1) / 2, and
+// the row and column terms carry the offsets.
+struct DensRowConst {
+  float mu, muh, mu_s, oxs;  // mu; mu_s (nu_size - 1) / 2; mu_s; sqrt(1 - mu^2) / ((nu_size - 1) / 2)
+  float offP, offE;          // (n - 1) / 2 - 1/2 of the nu and ground irradiance tables
+  float inv_h, c1;           // TWO: nu = w inv_h + c1
+  int nP, nE;                 // records per nu table row and of the ground irradiance table
+};
+template <bool TWO, bool GROUND, bool CL>
 __device__ __forceinline__ void dens_row(const DensLayout& S, const DensTheta& t, int l, int NT,
-                                         const LerpRec* __restrict__ Pl, const LerpRec* __restrict__ Ml, float mu,
-                                         float mu_s, float ox, const float (&sx)[kDensMaxGroup],
+                                         const LerpRec* __restrict__ Pl, const LerpRec* __restrict__ Ml,
+                                         const DensRowConst& q, const float (&sx)[kDensMaxGroup],
                                          const float (&sy)[kDensMaxGroup], int G, const PhaseCoef& pc, float kray,
-                                         float kmie, float nu_n1, float ir_n1, float3 (&acc)[kDensMaxGroup]) {
-  const float mus_ct = mu_s * t.cos_t, mu_ct = mu * t.cos_t;
+                                         float kmie, float3 (&acc)[kDensMaxGroup]) {
+  const float mus_ct = fmaf(q.muh, t.cos_t, q.offP), mu_ct = q.mu * t.cos_t;
   const float4* dirl = S.dir + l * NT;
   const float* gnzl = S.gnz + l * NT;
   for (int m = 0; m < NT; ++m) {
     const float4 d = dirl[m];
     // phase functions of omega . omega_i, shared by the pair and the group
-    const float nu2 = fmaf(ox, d.x, mu_ct);
+    const float nu2 = fmaf(q.oxs, d.x, mu_ct);
     const float3 cf = pc.eval(nu2, t.domega);
-    const float gzm = GROUND ? gnzl[m] * mu_s : 0.f;
+    const float gzm = GROUND ? fmaf(gnzl[m], q.mu_s, q.offE) : 0.f;
 #pragma unroll
     for (int j = 0; j < kDensMaxGroup; ++j) {
       if (j < G) {
@@ -870,32 +908,33 @@ __device__ __forceinline__ void dens_row(const DensLayout& S, const DensTheta& t
         const float gb = GROUND ? fmaf(d.z, sx[j], gzm) : 0.f, gdy = GROUND ? d.w * sy[j] : 0.f;
 #pragma unroll
         for (int side = 0; side < 2; ++side) {
-          const float nu1 = side ? base - dy : base + dy;
-          float lf;
-          const int k = lerp_pos(nu1, nu_n1, lf);
+          const float w = side ? base - dy : base + dy;
+          float fr;
+          const int k = mid_pos<CL>(w, q.nP, fr);
           const float4 pa = Pl[k].a;
           const float2 pb = Pl[k].b;
-          float3 inc = make_float3(fmaf(pa.w, lf, pa.x), fmaf(pb.x, lf, pa.y), fmaf(pb.y, lf, pa.z));
+          float3 inc = make_float3(fmaf(pa.w, fr, pa.x), fmaf(pb.x, fr, pa.y), fmaf(pb.y, fr, pa.z));
           if (TWO) {
+            const float nu1 = fmaf(w, q.inv_h, q.c1);
             const float4 qa = Ml[k].a;
             const float2 qb = Ml[k].b;
             const float pr = kray * fmaf(nu1, nu1, 1.0f);
             const float rs = rsqrtf(fmaf(-pc.g2, nu1, pc.g1));
             const float pm = kmie * fmaf(nu1, nu1, 1.0f) * (rs * rs * rs);
-            inc.x = fmaf(fmaf(qa.w, lf, qa.x), pm, inc.x * pr);
-            inc.y = fmaf(fmaf(qb.x, lf, qa.y), pm, inc.y * pr);
-            inc.z = fmaf(fmaf(qb.y, lf, qa.z), pm, inc.z * pr);
+            inc.x = fmaf(fmaf(qa.w, fr, qa.x), pm, inc.x * pr);
+            inc.y = fmaf(fmaf(qb.x, fr, qa.y), pm, inc.y * pr);
+            inc.z = fmaf(fmaf(qb.y, fr, qa.z), pm, inc.z * pr);
           }
           if (GROUND) {
             // irradiance of order n - 2 where omega_i meets the ground
-            const float mg = side ? gb - gdy : gb + gdy;
-            float lg;
-            const int e = lerp_pos(mg, ir_n1, lg);
+            const float we = side ? gb - gdy : gb + gdy;
+            float fe;
+            const int e = mid_pos<CL>(we, q.nE, fe);
             const float4 ea = S.E[e].a;
             const float2 eb = S.E[e].b;
-            inc.x = fmaf(t.tgx, fmaf(ea.w, lg, ea.x), inc.x);
-            inc.y = fmaf(t.tgy, fmaf(eb.x, lg, ea.y), inc.y);
-            inc.z = fmaf(t.tgz, fmaf(eb.y, lg, ea.z), inc.z);
+            inc.x = fmaf(t.tgx, fmaf(ea.w, fe, ea.x), inc.x);
+            inc.y = fmaf(t.tgy, fmaf(eb.x, fe, ea.y), inc.y);
+            inc.z = fmaf(t.tgz, fmaf(eb.y, fe, ea.z), inc.z);
           }
           acc[j].x = fmaf(inc.x, cf.x, acc[j].x);
           acc[j].y = fmaf(inc.y, cf.y, acc[j].y);
@@ -919,7 +958,7 @@ __device__ __forceinline__ void kahan_smem(volatile float* s, volatile float* c,
   *c = comp;
 }
 
-template <bool MX, bool TWO>
+template <bool MX, bool TWO, bool CL>
 __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned char* smem) {
   const int NT = a.dens_n, NNU = a.sc_nu, NK = NNU + 2;
   const DensShape sh = dens_shape(a.sc_r, a.sc_mu, a.sc_mus, a.sc_nu, a.dens_S, a.dens_chunk);
@@ -929,7 +968,7 @@ __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned cha
   const int ns = min(sh.S, a.sc_mus - s0), ny = min(sh.chunk, a.sc_mu - y0);
   const int tid = threadIdx.x, nth = blockDim.x;
   DensLayout S;
-  dens_layout(smem, NT, NNU, a.ir_mus, sh.S, sh.chunk, TWO, MX, &S);
+  dens_layout(smem, NT, NNU, a.ir_mus, sh.S, sh.chunk, TWO, MX, CL, &S);
 
   // --- tile scalars (r slice), theta rows, columns and mu rows from the
   // geometry tables
@@ -964,19 +1003,34 @@ __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned cha
   }
   __syncthreads();
   // --- reduced tables: the previous order's table at this tile's r and mu_s
-  // columns, on the theta rows, per nu slice (values first, then deltas to the
-  // next slice); direction pairs with ground normals; ground irradiance row
-  const size_t nPtab = (size_t)sh.S * NT * NK;
-  const int per_col = NT * NK;
+  // columns, on the theta rows, as nu intervals: the entries (pass 1), the
+  // differences (pass 2, into b and pad, which pass 1 readers do not touch),
+  // then midpoint and difference in place (pass 3); the same for the ground
+  // irradiance row; direction pairs with ground normals, pre-scaled for
+  // mid_pos
+  const int MK = dens_mk(NNU, CL), MKE = dens_mke(a.ir_mus, CL);
+  const size_t nPtab = (size_t)sh.S * NT * MK;
+  const int per_col = NT * MK;
+  const int ntab = TWO ? 2 : 1;
+  const float hP = 0.5f * float(NNU - 1), hE = 0.5f * float(a.ir_mus - 1);
   {
     const float4* src0 = TWO ? a.dr : a.dms;
     for (int k = tid; k < ns * per_col; k += nth) {
-      const int c = k / per_col, l = (k % per_col) / NK, sl = k % NK;
-      const float3 v = fetch3(src0, a.W, a.sc_mu, S.kax[c * NK + sl], S.tay[l], s_az);
+      const int c = k / per_col, l = (k % per_col) / MK, p = k % MK;
+      // interval ki (-1 .. nu_size): left entry nu slice ki, kax index ki + 1
+      const int ki = rec_interval<CL>(p, MK);
+      const bool used = ki <= NNU;
+      const int sl = ki + 1;
+      float3 v = make_float3(0.f, 0.f, 0.f), m = v;
+      if (used) {
+        v = fetch3(src0, a.W, a.sc_mu, S.kax[c * NK + sl], S.tay[l], s_az);
+        if (TWO) m = fetch3(a.dm, a.W, a.sc_mu, S.kax[c * NK + sl], S.tay[l], s_az);
+      }
       S.P[k].a = make_float4(v.x, v.y, v.z, 0.f);
+      S.P[k].b = S.P[k].pad = make_float2(0.f, 0.f);
       if (TWO) {
-        const float3 m = fetch3(a.dm, a.W, a.sc_mu, S.kax[c * NK + sl], S.tay[l], s_az);
         S.P[nPtab + k].a = make_float4(m.x, m.y, m.z, 0.f);
+        S.P[nPtab + k].b = S.P[nPtab + k].pad = make_float2(0.f, 0.f);
       }
     }
     const float dtheta = kPiF / float(NT), dphi = kPiF / float(NT);
@@ -989,33 +1043,57 @@ __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned cha
       const float dg = S.th[l].dg, ct = S.th[l].cos_t;
       const float gx = cx * dg, gy = cy * dg, gz = r + ct * dg;
       const float len = sqrtf(gx * gx + gy * gy + gz * gz);
-      S.dir[k] = make_float4(cx, cy, gx / len, gy / len);
-      S.gnz[k] = gz / len;
+      S.dir[k] = make_float4(cx * hP, cy * hP, gx / len * hE, gy / len * hE);
+      S.gnz[k] = gz / len * hE;
     }
+    // interval ki (entries ki, ki + 1) for ki < ir_mus; interval -1 (below
+    // entry 0) holds entry 0's value
     const float4* E = a.dirr[order & 1];  // irradiance of order n-2
     const float fy = s_irx.f;
-    for (int k = tid; k < a.ir_mus; k += nth) {
-      const float4 e0 = E[s_irx.i0 * a.ir_mus + k], e1 = E[s_irx.i1 * a.ir_mus + k];
-      S.E[k].a = make_float4(fmaf(e1.x - e0.x, fy, e0.x), fmaf(e1.y - e0.y, fy, e0.y), fmaf(e1.z - e0.z, fy, e0.z),
-                             0.f);
+    for (int k = tid; k < MKE; k += nth) {
+      const int ki = rec_interval<CL>(k, MKE);
+      const bool used = ki < a.ir_mus;
+      const int e = ki < 0 ? 0 : ki;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (used) {
+        const float4 e0 = E[s_irx.i0 * a.ir_mus + e], e1 = E[s_irx.i1 * a.ir_mus + e];
+        v = make_float4(fmaf(e1.x - e0.x, fy, e0.x), fmaf(e1.y - e0.y, fy, e0.y), fmaf(e1.z - e0.z, fy, e0.z), 0.f);
+      }
+      S.E[k].a = v;
+      S.E[k].b = S.E[k].pad = make_float2(0.f, 0.f);
     }
   }
   __syncthreads();
-  {  // deltas to the next slice / irradiance entry
+  {  // pass 2: differences of the two entries of each interval
     for (int k = tid; k < ns * per_col; k += nth) {
-      const bool last = (k % NK) == NK - 1;
-      for (int tb = 0; tb < (TWO ? 2 : 1); ++tb) {
-        const size_t o = tb * nPtab + k;
-        const float4 v0 = S.P[o].a, v1 = last ? v0 : S.P[o + 1].a;
-        S.P[o].b = make_float2(v1.y - v0.y, v1.z - v0.z);
-        S.P[o].a.w = v1.x - v0.x;
+      const int p = k % MK, row0 = k - p, ki = rec_interval<CL>(p, MK);
+      if (ki <= NNU - 1) {  // intervals -1 .. nu_size - 1
+        const int right = row0 + rec_pos<CL>(ki + 1, MK);
+        for (int tb = 0; tb < ntab; ++tb) {
+          const float4 v0 = S.P[tb * nPtab + k].a, v1 = S.P[tb * nPtab + right].a;
+          S.P[tb * nPtab + k].b = make_float2(v1.x - v0.x, v1.y - v0.y);
+          S.P[tb * nPtab + k].pad = make_float2(v1.z - v0.z, 0.f);
+        }
       }
     }
-    for (int k = tid; k < a.ir_mus; k += nth) {
-      const float4 v0 = S.E[k].a, v1 = k + 1 < a.ir_mus ? S.E[k + 1].a : v0;
-      S.E[k].b = make_float2(v1.y - v0.y, v1.z - v0.z);
-      S.E[k].a.w = v1.x - v0.x;
+    for (int k = tid; k < MKE; k += nth) {  // intervals 0 .. ir_mus - 2 (-1 and ir_mus - 1: flat)
+      const int ki = rec_interval<CL>(k, MKE);
+      if (ki >= 0 && ki <= a.ir_mus - 2) {
+        const float4 v0 = S.E[k].a, v1 = S.E[rec_pos<CL>(ki + 1, MKE)].a;
+        S.E[k].b = make_float2(v1.x - v0.x, v1.y - v0.y);
+        S.E[k].pad = make_float2(v1.z - v0.z, 0.f);
+      }
     }
+  }
+  __syncthreads();
+  {  // pass 3: midpoint value and difference, in the record's own fields
+    auto mid = [](LerpRec& rec) {
+      const float3 d = make_float3(rec.b.x, rec.b.y, rec.pad.x);
+      rec.a = make_float4(fmaf(0.5f, d.x, rec.a.x), fmaf(0.5f, d.y, rec.a.y), fmaf(0.5f, d.z, rec.a.z), d.x);
+      rec.b = make_float2(d.y, d.z);
+    };
+    for (int k = tid; k < ntab * ns * per_col; k += nth) mid(S.P[(k / (ns * per_col)) * nPtab + k % (ns * per_col)]);
+    for (int k = tid; k < MKE; k += nth) mid(S.E[k]);
   }
   __syncthreads();
 
@@ -1081,7 +1159,17 @@ __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned cha
     pc.B = make_float3(a.mie_sca[0] * rho_m * kmie, a.mie_sca[1] * rho_m * kmie, a.mie_sca[2] * rho_m * kmie);
     pc.g1 = 1.0f + g * g;
     pc.g2 = 2.0f * g;
-    const float nu_n1 = float(NNU - 1), ir_n1 = float(a.ir_mus - 1);
+    DensRowConst q;
+    q.mu = mu;
+    q.muh = mu_s * hP;
+    q.mu_s = mu_s;
+    q.oxs = ox / hP;
+    q.offP = hP - 0.5f;
+    q.offE = hE - 0.5f;
+    q.inv_h = 1.0f / hP;
+    q.c1 = 0.5f / hP - 1.0f;
+    q.nP = MK;
+    q.nE = MKE;
     float3 acc[kDensMaxGroup];
 #pragma unroll
     for (int j = 0; j < kDensMaxGroup; ++j) acc[j] = make_float3(0.f, 0.f, 0.f);
@@ -1094,13 +1182,12 @@ __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned cha
     }
     for (int l = 0; l < NT; ++l) {
       const DensTheta t = S.th[l];
-      // +1: the reduced table starts at nu slice -1
-      const LerpRec* Pl = S.P + (size_t)(cl * NT + l) * NK + 1;
+      const LerpRec* Pl = S.P + (size_t)(cl * NT + l) * MK;
       const LerpRec* Ml = Pl + nPtab;
       if (t.ground)
-        dens_row<TWO, true>(S, t, l, NT, Pl, Ml, mu, mu_s, ox, sx, sy, G, pc, kray, kmie, nu_n1, ir_n1, acc);
+        dens_row<TWO, true, CL>(S, t, l, NT, Pl, Ml, q, sx, sy, G, pc, kray, kmie, acc);
       else
-        dens_row<TWO, false>(S, t, l, NT, Pl, Ml, mu, mu_s, ox, sx, sy, G, pc, kray, kmie, nu_n1, ir_n1, acc);
+        dens_row<TWO, false, CL>(S, t, l, NT, Pl, Ml, q, sx, sy, G, pc, kray, kmie, acc);
       if (MX && ((l + 1) % kDensKahanRows == 0 || l == NT - 1)) {
         // Kahan sum over theta rows of the FP32 sums over kDensKahanRows rows
 #pragma unroll
@@ -1273,14 +1360,14 @@ __device__ void tile_indirect(const DevAtmo& a, int order, int tile, unsigned ch
 // V selects the occupancy variant chosen by the autotuner: V = 0 caps the
 // registers for 4 resident blocks per SM, V = 1 for 3, V = 2 for 5. TWO: the
 // launch of order 2, whose lookups read the single-scattering Rayleigh and
-// Mie tables.
-template <bool MX, int V, bool TWO>
+// Mie tables. CL: clamped interval tables (the largest sizes).
+template <bool MX, int V, bool TWO, bool CL>
 __global__ void __launch_bounds__(kDensThreads, V == 0 ? 4 : (V == 1 ? 3 : 5)) k_density(LaunchArgs L) {
   extern __shared__ __align__(16) unsigned char smem[];
   int seg, job, tile;
   int taken = 0;
   while (next_item(L, seg, job, tile, taken)) {
-    if (seg == 0) tile_density<MX, TWO>(L.atm[job], L.order, tile, smem);
+    if (seg == 0) tile_density<MX, TWO, CL>(L.atm[job], L.order, tile, smem);
     else tile_indirect<MX>(L.atm[job], L.order, tile, smem);
   }
 }
@@ -1543,9 +1630,12 @@ __host__ __device__ inline size_t ss_smem(int W, int steps, int sc_mus, int sc_n
   const int R = rows_per_tile(W);
   return align16(sizeof(RowGeo) * R) + sizeof(SSRec) * (size_t)R * (steps + 1);
 }
-__host__ __device__ inline size_t density_smem(const DevAtmo& a, bool two, bool mixed) {
+__host__ __device__ inline size_t density_smem(const DevAtmo& a, bool two, bool mixed, bool cl) {
   const DensShape d = dens_shape(a.sc_r, a.sc_mu, a.sc_mus, a.sc_nu, a.dens_S, a.dens_chunk);
-  return dens_layout(nullptr, a.dens_n, a.sc_nu, a.ir_mus, d.S, d.chunk, two, mixed, nullptr);
+  return dens_layout(nullptr, a.dens_n, a.sc_nu, a.ir_mus, d.S, d.chunk, two, mixed, cl, nullptr);
 }
+// Density variants: the occupancy variant (0..2), plus kDensClamped for the
+// clamped interval tables.
+constexpr int kDensClamped = 3;
 
 }  // namespace fb

@@ -244,3 +244,38 @@ def test_odd_sizes_match_oracle(builder, oracle, precision):
             assert ours["rms"] <= max(1.1 * ref32["rms"], PLAIN_RMS), (k, ours, ref32)
     else:
         _check(out, r64, keys, MIXED_MAX)
+
+
+def _clamped(**kw):
+    """A ground irradiance row of 4096 mu_s entries: its power-of-two interval
+    table (8192 records of 32 bytes) would not fit in shared memory, so the
+    density launches use the clamped interval tables."""
+    return smoke_parameters(**kw).replace(irradiance_mu_s_size=4096, irradiance_r_size=2)
+
+
+@pytest.mark.parametrize("precision", [0, PRECISION_MIXED])
+def test_clamped_interval_tables_match_oracle(builder, oracle, precision):
+    p = _clamped(order=3, precision=precision)
+    out = gpu_build(builder, p)
+    keys = ("transmittance", "irradiance", "scattering")
+    if precision == 0:
+        _check(out, oracle.precompute(p), keys, PLAIN_MAX, PLAIN_RMS)
+    else:
+        _check(out, oracle.precompute(p, dtype=np.float64), keys, MIXED_MAX)
+
+
+def test_batch_with_clamped_tables_equals_single_builds(builder):
+    """A density launch that needs the clamped tables for one atmosphere uses
+    them for the whole launch: the others get the same bits as their own
+    builds with the power-of-two tables."""
+    from fuzzyblue_gb300.api import build_batch
+    ps = [_clamped(order=3), smoke_parameters(order=3), tiny_parameters().replace(order=3),
+          _clamped(order=2, precision=PRECISION_MIXED), smoke_parameters(order=3, precision=PRECISION_MIXED)]
+    pend = build_batch(builder, ps)
+    pend.wait()
+    outs = [pend.atmosphere(i).to_host() for i in range(len(ps))]
+    pend.release()
+    for p, o in zip(ps, outs):
+        ref = gpu_build(builder, p)
+        for k in ("transmittance", "irradiance", "scattering"):
+            assert np.array_equal(o[k], ref[k]), k
