@@ -48,10 +48,15 @@ struct ColGeo {
   double mu_sd, one_m_mus2d, nu_rawd, t_musd;  // MIXED: FP64 values; t_musd = texel coordinate within a slice
 };
 
-// One trapezoid sample of multiple scattering along the view ray of a row.
-struct MSRec {
-  float d, inv_r, tvwx, tvwy, tvwz, fy, fz;  // distance, 1/r_i, transmittance x dx x weight, (mu, r) weights
-  int y0, y1, z0, z1, pad;
+// One trapezoid sample of multiple scattering along the view ray of a row:
+// distance, 1/r_i, transmittance x dx x trapezoid weight; the bilinear
+// weights and element offsets ((z sc_mu + y) W) of the four density rows
+// around the sample's (mu, r), corners (y0, z0), (y1, z0), (y0, z1), (y1, z1).
+struct __align__(16) MSRec {
+  float d, inv_r, tvwx, tvwy;
+  float tvwz, pad0, pad1, pad2;
+  float w[4];
+  int off[4];
 };
 
 // Scattering density: per r slice, and per (r slice, theta row) of the sphere grid.

@@ -380,7 +380,8 @@ __host__ __device__ inline int rows_per_tile(int W) { return W >= kThreads ? 1 :
 // multiple_scattering.comp:19-40, the parts that depend on the view ray and
 // the sample only (single-scattering launch, segment 2): the sample distance
 // and radius, the transmittance from the texel times dx and the trapezoid
-// weight, and the (mu, r) sampler axes of the density lookup.
+// weight, and the four density rows around the sample's (mu, r) with their
+// bilinear weights.
 template <bool MX> __device__ void tile_msrec(const DevAtmo& a, int tile) {
   const int NS = a.ms_steps + 1;
   const int k = tile * kThreads + threadIdx.x;
@@ -389,7 +390,7 @@ template <bool MX> __device__ void tile_msrec(const DevAtmo& a, int tile) {
   const int row = k / NS, i = k % NS, N = a.ms_steps;
   const RowGeo ri = a.g_rows[row];
   MSRec o;
-  o.pad = 0;
+  o.pad0 = o.pad1 = o.pad2 = 0.f;
   const float w = (i == 0 || i == N) ? 0.5f : 1.0f;
   float3 tv;
   Axis ay, az;
@@ -426,12 +427,14 @@ template <bool MX> __device__ void tile_msrec(const DevAtmo& a, int tile) {
   o.tvwx = tv.x * wdx;
   o.tvwy = tv.y * wdx;
   o.tvwz = tv.z * wdx;
-  o.y0 = ay.i0;
-  o.y1 = ay.i1;
-  o.fy = ay.f;
-  o.z0 = az.i0;
-  o.z1 = az.i1;
-  o.fz = az.f;
+  o.w[0] = (1.f - ay.f) * (1.f - az.f);
+  o.w[1] = ay.f * (1.f - az.f);
+  o.w[2] = (1.f - ay.f) * az.f;
+  o.w[3] = ay.f * az.f;
+  o.off[0] = (az.i0 * a.sc_mu + ay.i0) * a.W;
+  o.off[1] = (az.i0 * a.sc_mu + ay.i1) * a.W;
+  o.off[2] = (az.i1 * a.sc_mu + ay.i0) * a.W;
+  o.off[3] = (az.i1 * a.sc_mu + ay.i1) * a.W;
   a.g_ms[k] = o;
 }
 
@@ -1447,25 +1450,22 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
     const int b = k / (nrow * ng), rem = k % (nrow * ng);
     slab[b * slab_stride + (rem / ng) * SR + W + rem % ng] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
-  {  // this tile's sample records, their (mu, r) indices bounded to the table
-    static_assert(sizeof(MSRec) == 3 * sizeof(int4), "MSRec is three 16-byte words");
-    static_assert(offsetof(MSRec, y0) == 28 && offsetof(MSRec, y1) == 32 && offsetof(MSRec, z0) == 36 &&
-                      offsetof(MSRec, z1) == 40,
-                  "MSRec index words");
+  {  // this tile's sample records, their density row offsets bounded to the table
+    static_assert(sizeof(MSRec) == 4 * sizeof(int4) && offsetof(MSRec, off) == 3 * sizeof(int4),
+                  "MSRec: four 16-byte words, the offsets last");
     const int4* src = reinterpret_cast<const int4*>(a.g_ms + (size_t)row0 * NS);
     int4* dst = reinterpret_cast<int4*>(rec);
-    const int ymax = a.sc_mu - 1, zmax = a.sc_r - 1;
+    const int omax = (a.sc_r * a.sc_mu - 1) * W;  // start of the table's last row
     for (int k = tid; k < nrow * NS; k += nth) {
-      const int4 w0 = __ldg(src + 3 * k);
-      int4 w1 = __ldg(src + 3 * k + 1), w2 = __ldg(src + 3 * k + 2);
-      // words 7..10: y0, y1, z0, z1
-      w1.w = min(max(w1.w, 0), ymax);
-      w2.x = min(max(w2.x, 0), ymax);
-      w2.y = min(max(w2.y, 0), zmax);
-      w2.z = min(max(w2.z, 0), zmax);
-      dst[3 * k] = w0;
-      dst[3 * k + 1] = w1;
-      dst[3 * k + 2] = w2;
+      int4 o = __ldg(src + 4 * k + 3);
+      o.x = min(max(o.x, 0), omax);
+      o.y = min(max(o.y, 0), omax);
+      o.z = min(max(o.z, 0), omax);
+      o.w = min(max(o.w, 0), omax);
+      dst[4 * k] = __ldg(src + 4 * k);
+      dst[4 * k + 1] = __ldg(src + 4 * k + 1);
+      dst[4 * k + 2] = __ldg(src + 4 * k + 2);
+      dst[4 * k + 3] = o;
     }
   }
   // per-texel constants (TPT texels per thread): row, slab entry, texel x
@@ -1500,34 +1500,47 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
   }
   __syncthreads();
   const float4* dens = a.dens;
-  const size_t plane = (size_t)a.sc_mu * W;
   // Slab of sample i: the density table interpolated in (mu, r) at the
-  // sample, for the tile's slices of the row.
-  auto build = [&](int i, float4* dst) {
+  // sample, for the tile's slices of the row. With one texel per thread its
+  // four loads are issued one sample ahead (load) and blended after the texel
+  // work (blend); with more, the registers are not there and the loads
+  // directly precede the blend.
+  constexpr bool kAhead = TPT == 1;
+  float4 q[TPT][4];
+  auto load = [&](int i) {
 #pragma unroll
     for (int j = 0; j < TPT; ++j) {
-      if (tid + j * nth >= nx_tex) continue;
-      const int lr = c_lr[j], el = c_x[j], x = c_x[j];
-      const MSRec& o = rec[lr * NS + i];
-      const float4* p0 = dens + o.z0 * plane + x;
-      const float4* p1 = dens + o.z1 * plane + x;
-      const float4 a00 = ld4(p0 + (size_t)o.y0 * W), a10 = ld4(p0 + (size_t)o.y1 * W);
-      const float4 a01 = ld4(p1 + (size_t)o.y0 * W), a11 = ld4(p1 + (size_t)o.y1 * W);
-      const float w00 = (1.f - o.fy) * (1.f - o.fz), w10 = o.fy * (1.f - o.fz);
-      const float w01 = (1.f - o.fy) * o.fz, w11 = o.fy * o.fz;
-      float4 v;
-      v.x = fmaf(w11, a11.x, fmaf(w01, a01.x, fmaf(w10, a10.x, w00 * a00.x)));
-      v.y = fmaf(w11, a11.y, fmaf(w01, a01.y, fmaf(w10, a10.y, w00 * a00.y)));
-      v.z = fmaf(w11, a11.z, fmaf(w01, a01.z, fmaf(w10, a10.z, w00 * a00.z)));
-      v.w = 0.f;
-      dst[lr * SR + el] = v;
+      if (tid + j * nth < nx_tex) {
+        const MSRec& o = rec[c_lr[j] * NS + i];
+        const float4* p = dens + c_x[j];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) q[j][c] = ld4(p + o.off[c]);
+      }
     }
   };
-  build(0, slab);
+  auto blend = [&](int i, float4* dst) {
+#pragma unroll
+    for (int j = 0; j < TPT; ++j) {
+      if (tid + j * nth < nx_tex) {
+        const MSRec& o = rec[c_lr[j] * NS + i];
+        const float w00 = o.w[0], w10 = o.w[1], w01 = o.w[2], w11 = o.w[3];
+        const float4 a00 = q[j][0], a10 = q[j][1], a01 = q[j][2], a11 = q[j][3];
+        float4 v;
+        v.x = fmaf(w11, a11.x, fmaf(w01, a01.x, fmaf(w10, a10.x, w00 * a00.x)));
+        v.y = fmaf(w11, a11.y, fmaf(w01, a01.y, fmaf(w10, a10.y, w00 * a00.y)));
+        v.z = fmaf(w11, a11.z, fmaf(w01, a01.z, fmaf(w10, a10.z, w00 * a00.z)));
+        v.w = 0.f;
+        dst[c_lr[j] * SR + c_x[j]] = v;
+      }
+    }
+  };
+  load(0);
+  blend(0, slab);
   __syncthreads();
   const float fmus = float(NM);
   for (int i = 0; i < NS; ++i) {
     const float4* cur = slab + (i & 1) * slab_stride;
+    if (kAhead && i + 1 < NS) load(i + 1);
 #pragma unroll
     for (int j = 0; j < TPT; ++j) {
       if (tid + j * nth < nx_tex) {
@@ -1565,7 +1578,10 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
         }
       }
     }
-    if (i + 1 < NS) build(i + 1, slab + ((i + 1) & 1) * slab_stride);
+    if (i + 1 < NS) {
+      if (!kAhead) load(i + 1);
+      blend(i + 1, slab + ((i + 1) & 1) * slab_stride);
+    }
     __syncthreads();
   }
   // outputs: delta multiple scattering and the final table (:91-92)
