@@ -268,28 +268,53 @@ def run_ours(a):
     torch.cuda.synchronize()
     graph_ms = max_over_ranks(world, g0.elapsed_time(g1)) / a.steps
 
-    # end to end through the public API with host buffers
+    # end to end through the public API with host buffers: every step's
+    # parameters go in with its build and all three tables of every
+    # atmosphere come back into page-locked host memory
+    # (fb_atmosphere_copy_to_host_async). Two steps are in flight on two
+    # streams, each with its own host buffer: a step's build waits on the
+    # device for the previous build (fb_pending_acquire), so builds run back
+    # to back while each step's copies overlap the next step's kernels; the
+    # timed region ends when the last copy is done.
     sizes = params[0].texel_counts()
     per_atm = 16 * sum(sizes)
-    host = torch.empty((a.batch, per_atm // 4), dtype=torch.float32, pin_memory=True).numpy()
+    hosts = [torch.empty((a.batch, per_atm // 4), dtype=torch.float32, pin_memory=True).numpy() for _ in range(2)]
+    streams = [stream, torch.cuda.Stream()]
     tw, th = params[0].transmittance_extent()
     iw, ih = params[0].irradiance_extent()
     n_tr, n_ir = 4 * tw * th, 4 * iw * ih
-    import ctypes
     from fuzzyblue_gb300 import _native as N
     h2d = a.batch * 384
+    inflight = [None, None]
+    # untimed: one build on each stream, so that the memory pool holds two
+    # batches' tables and temporaries before the timed steps
+    warm = [build_batch(builder, params, stream=streams[k]) for k in (0, 1)]
+    for w in warm:
+        w.wait()
+        w.release()
     barrier(world)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(a.steps):
-        p = build_batch(builder, params, stream=stream)
-        p.wait()
+    prev = None
+    for s in range(a.steps):
+        k = s & 1
+        if inflight[k] is not None:  # that stream's previous step: copies done, then release
+            streams[k].synchronize()
+            inflight[k].release()
+        if prev is not None:
+            prev.acquire(streams[k])
+        p = build_batch(builder, params, stream=streams[k])
+        prev = p
         for i in range(a.batch):
-            base = host[i].ctypes.data
-            atm = p.atmosphere(i)
-            N.check(N.lib().fb_atmosphere_copy_to_host(atm._h, stream.cuda_stream, base, base + 4 * n_tr,
-                                                       base + 4 * (n_tr + n_ir)), "copy_to_host")
-        p.release()
+            base = hosts[k][i].ctypes.data
+            N.check(N.lib().fb_atmosphere_copy_to_host_async(p.atmosphere(i)._h, streams[k].cuda_stream, base,
+                                                             base + 4 * n_tr, base + 4 * (n_tr + n_ir)),
+                    "fb_atmosphere_copy_to_host_async")
+        inflight[k] = p
+    for k in (0, 1):
+        streams[k].synchronize()
+        if inflight[k] is not None:
+            inflight[k].release()
     torch.cuda.synchronize()
     e2e_s = max_over_ranks(world, time.perf_counter() - t0) / a.steps
     e2e = world * a.batch / e2e_s
@@ -353,7 +378,8 @@ def run_ours(a):
                        a.batch * 0.1)},
         "clocks": clk,
         "e2e": {"value": e2e, "unit": "atmospheres/s", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": a.batch * per_atm},
+                "d2h_bytes_per_step": a.batch * per_atm,
+                "overlap": "two steps in flight on two streams: one step's copies overlap the next step's kernels"},
         "gpu_launches": sum(len(x) for x in prof),
         "roofline": {"bound": "fp32", "kernel": "k_density (scattering density + indirect irradiance), order >= 3",
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s",

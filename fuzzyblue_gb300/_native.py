@@ -145,6 +145,7 @@ SIGNATURES = {
     "fb_pending_release": (None, [_V]),
     "fb_atmosphere_tables": (_I, [_V, ctypes.POINTER(c_tables)]),
     "fb_atmosphere_copy_to_host": (_I, [_V, _V, _V, _V, _V]),
+    "fb_atmosphere_copy_to_host_async": (_I, [_V, _V, _V, _V, _V]),
     "fb_atmosphere_export_scattering_f16": (_I, [_V, _V, _V]),
     "fb_atmosphere_params": (_I, [_V, _P]),
     "fb_atmosphere_destroy": (None, [_V]),

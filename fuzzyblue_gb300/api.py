@@ -190,6 +190,26 @@ class Atmosphere:
                                                    out["scattering"].ctypes.data), "fb_atmosphere_copy_to_host")
         return out
 
+    def copy_to_host_async(self, transmittance, irradiance, scattering, stream=None):
+        """Enqueues the copies of the three tables into host buffers (any of
+        them None to skip) on `stream` and returns at once; the buffers hold
+        the tables once the stream has passed this point. Numpy arrays must be
+        contiguous float32 of the table sizes; page-locked memory (e.g. a
+        pinned torch tensor's numpy view) keeps the copies asynchronous."""
+        def ptr(x):
+            if x is None:
+                return None
+            assert x.dtype == np.float32 and x.flags["C_CONTIGUOUS"]
+            return x.ctypes.data
+        tw, th = self.params.transmittance_extent()
+        iw, ih = self.params.irradiance_extent()
+        sw, sh, sd = self.params.scattering_extent()
+        for x, n in ((transmittance, tw * th), (irradiance, iw * ih), (scattering, sw * sh * sd)):
+            assert x is None or x.size >= 4 * n, "host buffer too small"
+        N.check(N.lib().fb_atmosphere_copy_to_host_async(self._h, _stream_handle(stream), ptr(transmittance),
+                                                         ptr(irradiance), ptr(scattering)),
+                "fb_atmosphere_copy_to_host_async")
+
     def render_sky(self, draw, width: int, height: int, depth=None, stream=None):
         """The crate's sky pass for a width x height image (fuzzyblue_gb300.render)."""
         from .render import render_sky

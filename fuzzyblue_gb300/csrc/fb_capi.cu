@@ -438,6 +438,18 @@ extern "C" int fb_atmosphere_copy_to_host(const fb_atmosphere* a, void* stream, 
   return FB_OK;
 }
 
+extern "C" int fb_atmosphere_copy_to_host_async(const fb_atmosphere* a, void* stream, float* tr, float* ir,
+                                                float* sc) {
+  if (!a) return fail(FB_ERR_INVALID_ARGUMENT, "atmosphere is NULL");
+  FB_CU(cudaSetDevice(a->b->device));
+  cudaStream_t s = stream ? (cudaStream_t)stream : a->b->stream;
+  fbi::TableSizes z = fbi::sizes_of(a->params);
+  if (tr) FB_CU(cudaMemcpyAsync(tr, a->tr, 16 * z.ntr, cudaMemcpyDeviceToHost, s));
+  if (ir) FB_CU(cudaMemcpyAsync(ir, a->ir, 16 * z.nir, cudaMemcpyDeviceToHost, s));
+  if (sc) FB_CU(cudaMemcpyAsync(sc, a->sc, 16 * z.nsc, cudaMemcpyDeviceToHost, s));
+  return FB_OK;
+}
+
 extern "C" int fb_atmosphere_export_scattering_f16(const fb_atmosphere* a, void* stream, uint16_t* out) {
   if (!a || !out) return fail(FB_ERR_INVALID_ARGUMENT, "NULL argument");
   FB_CU(cudaSetDevice(a->b->device));

@@ -241,6 +241,14 @@ int fb_atmosphere_tables(const fb_atmosphere* a, fb_tables* out);
 int fb_atmosphere_copy_to_host(const fb_atmosphere* a, void* stream,
                                float* transmittance, float* irradiance,
                                float* scattering);
+/* The same copies, enqueued on `stream` without waiting: the host buffers
+ * hold the tables once the stream has passed this point (synchronize the
+ * stream, or wait on an event recorded after the call). Asynchronous with
+ * respect to the host only for page-locked host buffers. Lets a caller
+ * overlap the copies of one build with the kernels of the next. */
+int fb_atmosphere_copy_to_host_async(const fb_atmosphere* a, void* stream,
+                                     float* transmittance, float* irradiance,
+                                     float* scattering);
 /* RGBA16F copy of the scattering table (the reference's image format,
  * src/precompute.rs:1215; examples/dump.rs:120): `out` holds
  * width*height*depth*4 uint16 half floats, round to nearest even. */

@@ -241,6 +241,8 @@ extern "C" {
     pub fn fb_atmosphere_tables(a: *const fb_atmosphere, out: *mut fb_tables) -> c_int;
     pub fn fb_atmosphere_copy_to_host(a: *const fb_atmosphere, stream: *mut c_void, tr: *mut f32,
                                       ir: *mut f32, sc: *mut f32) -> c_int;
+    pub fn fb_atmosphere_copy_to_host_async(a: *const fb_atmosphere, stream: *mut c_void, tr: *mut f32,
+                                            ir: *mut f32, sc: *mut f32) -> c_int;
     pub fn fb_atmosphere_export_scattering_f16(a: *const fb_atmosphere, stream: *mut c_void,
                                                out: *mut u16) -> c_int;
     pub fn fb_atmosphere_params(a: *const fb_atmosphere, out: *mut fb_params) -> c_int;

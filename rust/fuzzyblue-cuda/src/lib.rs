@@ -366,6 +366,15 @@ impl Atmosphere {
         Ok((t, i, s))
     }
 
+    /// Enqueues the copies of the three tables into caller-owned host buffers
+    /// on `stream` without waiting; the buffers hold the tables once the
+    /// stream has passed this point (page-locked buffers for the copies to be
+    /// asynchronous). Any pointer may be null.
+    pub unsafe fn copy_to_host_async(&self, stream: Stream, transmittance: *mut f32, irradiance: *mut f32,
+                                     scattering: *mut f32) -> Result<(), Error> {
+        check(sys::fb_atmosphere_copy_to_host_async(self.raw, stream.0, transmittance, irradiance, scattering))
+    }
+
     /// The crate's sky pass (render_sky.frag) for a width x height image into
     /// device buffers of RGBA f32 (`transmittance` may be null); `depth` is a
     /// device buffer of width * height floats or null (nothing in front of the sky).

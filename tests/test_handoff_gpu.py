@@ -49,3 +49,31 @@ def test_build_on_a_caller_stream_then_query(builder):
     s.synchronize()
     assert pend.query()
     pend.release()
+
+
+def test_async_copies_overlap_the_next_build(builder):
+    """fb_atmosphere_copy_to_host_async enqueues the copies without a host
+    wait: a build's copies on one stream and the next build on another give
+    host tables equal to the blocking copy of the same atmospheres."""
+    import torch
+    s0, s1 = torch.cuda.Stream(), torch.cuda.Stream()
+    params = [tiny_parameters().replace(order=3), smoke_parameters(precision=PRECISION_MIXED, order=4)]
+    first = _build(builder, params, s0)
+    hosts = []
+    for i, p in enumerate(params):
+        tw, th = p.transmittance_extent()
+        iw, ih = p.irradiance_extent()
+        sw, sh, sd = p.scattering_extent()
+        h = {k: torch.empty(n * 4, dtype=torch.float32, pin_memory=True).numpy()
+             for k, n in (("transmittance", tw * th), ("irradiance", iw * ih), ("scattering", sw * sh * sd))}
+        first.atmosphere(i).copy_to_host_async(h["transmittance"], h["irradiance"], h["scattering"], stream=s0)
+        hosts.append(h)
+    second = _build(builder, list(reversed(params)), s1)  # runs while the copies are in flight
+    s0.synchronize()
+    for i in range(len(params)):
+        ref = first.atmosphere(i).to_host()
+        for k in ("transmittance", "irradiance", "scattering"):
+            assert np.array_equal(hosts[i][k], ref[k].reshape(-1)), k
+    second.wait()
+    first.release()
+    second.release()
