@@ -541,9 +541,15 @@ __host__ __device__ inline int tiles_densgeo(int sc_r, int dens_n) {
 }
 
 // ============================================================ S: single ===
-struct SSRec {
-  float d, r_d, inv_r, rr_d, dmin, inv_span, tvx, tvy, tvz, rho_r, rho_m, w, cos_h, lo, inv_w, fy, e;
-  int y0, y1;
+// Per (row, sample) of single scattering; 16-byte words in the order the
+// texel loop reads them, so that each is one shared load.
+struct __align__(16) SSRec {
+  float d, inv_r, r_d, rr_d;
+  float e, dmin, inv_span, cos_h;
+  float lo, inv_w, fy, w;
+  float tvx, tvy, tvz, rho_r;
+  float rho_m;
+  int y0, y1, pad;
 };
 
 
@@ -565,6 +571,7 @@ __device__ void tile_single(const DevAtmo& a, int tile, unsigned char* smem) {
     const RowGeo& ri = rows[k / NS];
     const int i = k % NS;
     SSRec& o = rec[k];
+    o.pad = 0;
     o.w = (i == 0 || i == N) ? 0.5f : 1.0f;
     float3 tv;
     if (!MX) {
