@@ -900,8 +900,8 @@ template <bool TWO, bool GROUND, bool CL>
 __device__ __forceinline__ void dens_row(const DensLayout& S, const DensTheta& t, int l, int NT,
                                          const LerpRec* __restrict__ Pl, const LerpRec* __restrict__ Ml,
                                          const DensRowConst& q, const float (&sx)[kDensMaxGroup],
-                                         const float (&sy)[kDensMaxGroup], int G, const PhaseCoef& pc, float kray,
-                                         float kmie, float3 (&acc)[kDensMaxGroup]) {
+                                         const float (&sy)[kDensMaxGroup], int G, const PhaseCoef& pc,
+                                         float3 (&acc)[kDensMaxGroup]) {
   const float mus_ct = fmaf(q.muh, t.cos_t, q.offP), mu_ct = q.mu * t.cos_t;
   const float4* dirl = S.dir + l * NT;
   const float* gnzl = S.gnz + l * NT;
@@ -925,15 +925,17 @@ __device__ __forceinline__ void dens_row(const DensLayout& S, const DensTheta& t
           const float2 pb = Pl[k].b;
           float3 inc = make_float3(fmaf(pa.w, fr, pa.x), fmaf(pb.x, fr, pa.y), fmaf(pb.y, fr, pa.z));
           if (TWO) {
+            // R P_R(nu) + M P_M(nu) = (1 + nu^2) (kR R + kM (1 + g^2 - 2 g nu)^-3/2 M),
+            // the constants kR, kM folded into the tables
             const float nu1 = fmaf(w, q.inv_h, q.c1);
             const float4 qa = Ml[k].a;
             const float2 qb = Ml[k].b;
-            const float pr = kray * fmaf(nu1, nu1, 1.0f);
+            const float t1 = fmaf(nu1, nu1, 1.0f);
             const float rs = rsqrtf(fmaf(-pc.g2, nu1, pc.g1));
-            const float pm = kmie * fmaf(nu1, nu1, 1.0f) * (rs * rs * rs);
-            inc.x = fmaf(fmaf(qa.w, fr, qa.x), pm, inc.x * pr);
-            inc.y = fmaf(fmaf(qb.x, fr, qa.y), pm, inc.y * pr);
-            inc.z = fmaf(fmaf(qb.y, fr, qa.z), pm, inc.z * pr);
+            const float rs3 = rs * rs * rs;
+            inc.x = fmaf(fmaf(qa.w, fr, qa.x), rs3, inc.x) * t1;
+            inc.y = fmaf(fmaf(qb.x, fr, qa.y), rs3, inc.y) * t1;
+            inc.z = fmaf(fmaf(qb.y, fr, qa.z), rs3, inc.z) * t1;
           }
           if (GROUND) {
             // irradiance of order n - 2 where omega_i meets the ground
@@ -1025,6 +1027,10 @@ __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned cha
   const float hP = 0.5f * float(NNU - 1), hE = 0.5f * float(a.ir_mus - 1);
   {
     const float4* src0 = TWO ? a.dr : a.dms;
+    // order 2: the Rayleigh and Mie tables carry their phase functions'
+    // constants, 3 / (16 pi) and 3 / (8 pi) (1 - g^2) / (2 + g^2)
+    const float sR = TWO ? 3.0f / (16.0f * kPiF) : 1.0f;
+    const float sM = 3.0f / (8.0f * kPiF) * (1.0f - a.g * a.g) / (2.0f + a.g * a.g);
     for (int k = tid; k < ns * per_col; k += nth) {
       const int c = k / per_col, l = (k % per_col) / MK, p = k % MK;
       // interval ki (-1 .. nu_size): left entry nu slice ki, kax index ki + 1
@@ -1033,8 +1039,8 @@ __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned cha
       const int sl = ki + 1;
       float3 v = make_float3(0.f, 0.f, 0.f), m = v;
       if (used) {
-        v = fetch3(src0, a.W, a.sc_mu, S.kax[c * NK + sl], S.tay[l], s_az);
-        if (TWO) m = fetch3(a.dm, a.W, a.sc_mu, S.kax[c * NK + sl], S.tay[l], s_az);
+        v = fetch3(src0, a.W, a.sc_mu, S.kax[c * NK + sl], S.tay[l], s_az) * sR;
+        if (TWO) m = fetch3(a.dm, a.W, a.sc_mu, S.kax[c * NK + sl], S.tay[l], s_az) * sM;
       }
       S.P[k].a = make_float4(v.x, v.y, v.z, 0.f);
       S.P[k].b = S.P[k].pad = make_float2(0.f, 0.f);
@@ -1195,9 +1201,9 @@ __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned cha
       const LerpRec* Pl = S.P + (size_t)(cl * NT + l) * MK;
       const LerpRec* Ml = Pl + nPtab;
       if (t.ground)
-        dens_row<TWO, true, CL>(S, t, l, NT, Pl, Ml, q, sx, sy, G, pc, kray, kmie, acc);
+        dens_row<TWO, true, CL>(S, t, l, NT, Pl, Ml, q, sx, sy, G, pc, acc);
       else
-        dens_row<TWO, false, CL>(S, t, l, NT, Pl, Ml, q, sx, sy, G, pc, kray, kmie, acc);
+        dens_row<TWO, false, CL>(S, t, l, NT, Pl, Ml, q, sx, sy, G, pc, acc);
       if (MX && ((l + 1) % kDensKahanRows == 0 || l == NT - 1)) {
         // Kahan sum over theta rows of the FP32 sums over kDensKahanRows rows
 #pragma unroll
