@@ -621,7 +621,8 @@ void plan_group(Plan& P, const std::vector<DevAtmo>& A, const std::vector<int>& 
     }
     add_segment(P, M, 0, jobs, tm);
     M.nseg = 1;
-    M.variant = M.block > fb::kThreads ? 2 : launch_variant(A, jobs, tun, mixed, false);
+    M.variant = fb::ms_block_variant(M.block) >= 0 ? fb::ms_block_variant(M.block)
+                                                   : launch_variant(A, jobs, tun, mixed, false);
     P.launches.push_back(M);
   }
 }

@@ -10,7 +10,8 @@ enum PassKind { kPassTransmittance = 0, kPassSingle = 1, kPassDensity = 2, kPass
 
 // Kernel of (mode, pass, texels-per-thread, variant, order 2). Multiple
 // scattering: variant 0 / 1 = CTAs of kThreads with registers for 4 / 3 CTAs
-// per SM (tpt 1), variant 2 = CTAs of kMsWideThreads (tpt 1 or 2). Density:
+// per SM (tpt 1), variant 2 / 3 = CTAs of kMsWideThreads / kMsMidThreads
+// (tpt 1 or 2). Density:
 // variant 0 / 1 = registers for 4 / 3 CTAs per SM; order2 selects the launch
 // of order 2 (it reads the single-scattering tables).
 const void* kernel_plain(int pass, int tpt, int variant, bool order2);

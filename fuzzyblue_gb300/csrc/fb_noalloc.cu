@@ -203,7 +203,7 @@ extern "C" int fb_atmosphere_build_noalloc(void* stream, const fb_params* p, voi
         cl ? fb::kDensClamped : 0);
     add(fb::kPassMultiple, n, {fb::tiles_multiple(d.W, d.sc_mus, d.ms_steps, d.sc_mu, d.sc_r, ms_block)},
         fb::ms_smem(d.W, d.ms_steps, d.sc_mus, ms_block), fb::ms_shape(d.W, d.sc_mus, d.ms_steps, ms_block).TPT, ms_block,
-        ms_block > fb::kThreads ? 2 : 0);
+        std::max(0, fb::ms_block_variant(ms_block)));
   }
   cudaError_t e = cudaMemcpyAsync(base + o_atm, &d, sizeof(d), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess)

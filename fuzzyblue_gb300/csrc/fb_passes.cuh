@@ -1399,10 +1399,12 @@ __global__ void __launch_bounds__(kDensThreads, V == 0 ? 4 : (V == 1 ? 3 : 5)) k
 // Tile of multiple scattering: whole rows (a texel's lookups can reach any
 // nu slice of its row: its clamped nu picks the slices), R = threads / W rows
 // per CTA for rows of at most `threads` texels, else one row with TPT texels
-// per thread. Launches use CTAs of kThreads threads, or of kMsWideThreads when
-// a row of the launch is wider than kThreads. The slab of a row holds the row
-// plus a zero guard nu slice, read with weight 0 where nu = 1 selects the
-// last slice.
+// per thread. Launches use CTAs of kThreads threads; when a row of the launch
+// is wider, CTAs of kMsMidThreads (two per SM, so that one runs while the
+// other waits at its per-sample barrier) up to rows of 1024 texels, else of
+// kMsWideThreads. The slab of a row holds the row plus a zero guard nu slice,
+// read with weight 0 where nu = 1 selects the last slice.
+constexpr int kMsMidThreads = 512;
 constexpr int kMsWideThreads = 1024;
 constexpr int kMsRowBytes = 96 * 1024;  // shared memory for the rows of a tile (records + slabs)
 struct MSShape {
@@ -1419,7 +1421,14 @@ __host__ __device__ inline MSShape ms_shape(int W, int sc_mus, int steps, int th
   return m;
 }
 // CTA size of a launch over rows of width W (the widest of the launch).
-__host__ __device__ inline int ms_threads(int W) { return W <= kThreads ? kThreads : kMsWideThreads; }
+__host__ __device__ inline int ms_threads(int W) {
+  return W <= kThreads ? kThreads : (W <= 2 * kMsMidThreads ? kMsMidThreads : kMsWideThreads);
+}
+// Kernel variant of a launch of `block` threads: 2 and 3 for the wide CTA
+// sizes, -1 for kThreads (the tuned occupancy variant 0 or 1 applies).
+__host__ __device__ inline int ms_block_variant(int block) {
+  return block == kMsWideThreads ? 2 : (block == kMsMidThreads ? 3 : -1);
+}
 __host__ __device__ inline int tiles_multiple(int W, int sc_mus, int steps, int sc_mu, int sc_r, int threads) {
   const MSShape m = ms_shape(W, sc_mus, steps, threads);
   return (sc_mu * sc_r + m.R - 1) / m.R;
@@ -1629,9 +1638,11 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
 }
 
 // V = 0: CTAs of kThreads, registers capped for 4 resident CTAs per SM;
-// V = 1: for 3; V = 2: CTAs of kMsWideThreads (rows wider than kThreads).
+// V = 1: for 3; V = 2: CTAs of kMsWideThreads, one per SM; V = 3: CTAs of
+// kMsMidThreads, two per SM.
 template <bool MX, int TPT, int V>
-__global__ void __launch_bounds__(V == 2 ? kMsWideThreads : kThreads, V == 2 ? 1 : (V == 0 ? 4 : 3))
+__global__ void __launch_bounds__(V == 2 ? kMsWideThreads : (V == 3 ? kMsMidThreads : kThreads),
+                                  V == 2 ? 1 : (V == 3 ? 2 : (V == 0 ? 4 : 3)))
     k_multiple(LaunchArgs L) {
   extern __shared__ __align__(16) unsigned char smem[];
   int seg, job, tile;
