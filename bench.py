@@ -121,26 +121,18 @@ class Clocks:
 
 # ------------------------------------------------------------ distributed --
 def dist():
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return world, rank, local
+    from fuzzyblue_gb300.ranks import layout
+    return layout()
 
 
 def barrier(world):
-    if world > 1:
-        import torch.distributed as td
-        td.barrier()
+    from fuzzyblue_gb300.ranks import barrier as rank_barrier
+    rank_barrier(world)
 
 
 def max_over_ranks(world, v):
-    if world == 1:
-        return v
-    import torch
-    import torch.distributed as td
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
-    td.all_reduce(t, op=td.ReduceOp.MAX)
-    return float(t.item())
+    from fuzzyblue_gb300.ranks import max_over_ranks as rank_max
+    return rank_max(world, v)
 
 
 # ------------------------------------------------------------- roofline ---
@@ -253,7 +245,8 @@ def run_ours(a):
     clk = clocks.stop()
     total_ms = max_over_ranks(world, ev0.elapsed_time(ev1))
     ms_per_step = total_ms / a.steps
-    value = world * a.batch / (ms_per_step / 1e3)
+    from fuzzyblue_gb300.ranks import whole_job_rate
+    value = whole_job_rate(world, a.batch, ms_per_step / 1e3)
 
     # the same steps replayed from the CUDA graph (no per-launch events)
     builder.set_profiling(False)
@@ -317,7 +310,7 @@ def run_ours(a):
             inflight[k].release()
     torch.cuda.synchronize()
     e2e_s = max_over_ranks(world, time.perf_counter() - t0) / a.steps
-    e2e = world * a.batch / e2e_s
+    e2e = whole_job_rate(world, a.batch, e2e_s)
 
     # plain path: one default-size atmosphere per call, FP32
     plain_p = Parameters()
