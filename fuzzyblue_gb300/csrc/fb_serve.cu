@@ -8,7 +8,8 @@
 // it), moving their tables into the resident cache and freeing their
 // temporaries; (2) while a stream is free, picks the request that leads its
 // batch - on a high-priority stream the oldest cheap request, on a
-// low-priority stream the oldest request of any class - adds the queued
+// low-priority stream the oldest request of any class, an expensive one only
+// while no other expensive batch runs - adds the queued
 // requests of the lead's table class in arrival order while the budget
 // (evicting unpinned resident tables, least recently used first) and the
 // batch's estimated duration allow, and launches them as one batch build
@@ -75,6 +76,7 @@ struct Batch {
   size_t bytes = 0;
   double cost = 0;      // texel-orders
   double t_launch = 0;  // ms
+  bool expensive = false;  // led by a request above the cheap threshold
   bool has_callback = false;      // completion is signalled by the host callback
   std::atomic<bool> done{false};  // set by that callback as its last action
 };
@@ -289,6 +291,10 @@ bool pick_lead(fb_server* s, int& slot, uint64_t& lead, bool& cheap_only) {
   const double now = now_ms();
   const bool high_for_all = !any_low;
   const bool hold_high = !high_for_all && low_priority_starved(s, now);
+  // one expensive batch at a time: it fills the GPU alone, and a second one
+  // beside it would only stretch both (they run in arrival order instead)
+  bool expensive_running = false;
+  for (const Batch* bt : s->inflight) expensive_running |= bt->expensive;
   size_t seen = 0;
   bool oldest = true;
   for (auto qi = s->queue.begin(); qi != s->queue.end() && seen < kLeadScan;) {
@@ -317,7 +323,7 @@ bool pick_lead(fb_server* s, int& slot, uint64_t& lead, bool& cheap_only) {
       cheap_only = !high_for_all;
       return true;
     }
-    if (free_low >= 0) {
+    if (free_low >= 0 && (cheap || high_for_all || !expensive_running)) {
       slot = free_low;
       lead = t;
       cheap_only = false;
@@ -400,6 +406,7 @@ void admit(fb_server* s) {
     bt->bytes = bytes;
     bt->cost = cost;
     bt->t_launch = now_ms();
+    bt->expensive = cost_of(head) > kCheapBatch;
     s->stream_busy[slot] = true;
     s->inflight_bytes += bytes;
     s->inflight.push_back(bt);
