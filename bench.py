@@ -52,9 +52,10 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "plain"],
                     help="arithmetic of the batch (the headline is mixed)")
-    ap.add_argument("--workload", default="uniform", choices=["uniform", "uneven", "serve"],
+    ap.add_argument("--workload", default="uniform", choices=["uniform", "uneven", "serve", "render"],
                     help="uniform: the headline batch; uneven: 96 atmospheres over three table classes, "
-                         "orders 2-8; serve: open-loop Poisson requests through the request loop")
+                         "orders 2-8; serve: open-loop Poisson requests through the request loop; "
+                         "render: the headless sky pass over the tables, 1920x1080 frames")
     ap.add_argument("--rates", default="50,200,1000", help="serve: offered request rates (req/s)")
     ap.add_argument("--duration", type=float, default=60.0, help="serve: seconds of arrivals per rate")
     ap.add_argument("--max-queue", type=int, default=512,
@@ -452,6 +453,138 @@ def run_reference(a):
     print(json.dumps(out))
 
 
+# ---------------------------------------------------------------- render ---
+RENDER_W, RENDER_H = 1920, 1080
+
+
+def render_scene(p):
+    """Camera 1 km above the ground looking just above the horizon, the sun
+    45 degrees up; depth: a seeded half of the pixels at finite depth (aerial
+    perspective, 20 m to 5 km), the rest sky."""
+    import numpy as np
+    from fuzzyblue_gb300.render import DrawParameters
+    d = DrawParameters.look_at((0.0, p.bottom_radius + 1.0, 0.0), forward=(1.0, 0.15, 0.3), up=(0, 1, 0),
+                               fov_y_deg=70.0, aspect=RENDER_W / RENDER_H, sun_direction=(0.4, 0.7071, 0.58))
+    rng = np.random.default_rng(3)
+    depth = np.where(rng.random((RENDER_H, RENDER_W)) < 0.5,
+                     rng.uniform(2e-5, 5e-3, (RENDER_H, RENDER_W)), 0.0).astype(np.float32)
+    return d, depth
+
+
+def run_render(a):
+    """The headless sky pass of the crate's renderer (render_sky.frag over
+    render_sky.h; fb_atmosphere_render_sky) over the tables of one default
+    atmosphere (uniform batch seed 0, mixed precision): one 1920x1080 frame per
+    step, radiance and transmittance written as float4. value: device-resident
+    frames; e2e: the depth buffer copied in from pinned host memory and the
+    radiance copied out every frame. CPU baseline: the reference's own shading
+    code compiled as C++ (oracle/_ref), all host cores, on a 240x135 frame of
+    the same view, scaled by the pixel count."""
+    world, rank, local = dist()
+    import numpy as np
+    import torch
+    torch.cuda.set_device(local)
+    from fuzzyblue_gb300 import workloads
+    from fuzzyblue_gb300.api import Atmosphere, Builder
+    from fuzzyblue_gb300.params import PRECISION_MIXED
+    from fuzzyblue_gb300.render import render_sky
+    builder = Builder(local)
+    p = workloads.uniform_batch(1, seed=0, order=ORDERS, precision=PRECISION_MIXED)[0]
+    pend = Atmosphere.build(builder, p)
+    pend.wait()
+    atm = pend.take(0)
+    pend.release()
+    draw, depth_h = render_scene(p)
+    stream = torch.cuda.Stream()
+    depth = torch.as_tensor(depth_h).to("cuda")
+    for _ in range(max(a.warmup, 3)):
+        render_sky(atm, draw, RENDER_W, RENDER_H, depth=depth, stream=stream)
+    stream.synchronize()
+    # Frames are short (well under a millisecond) and the tables fit in L2, so
+    # each timed frame has its own events and a 256 MB write between frames,
+    # outside them, evicts the tables and buffers from L2 (cold tables every
+    # frame); enough frames for the clock sampler to see the timed region.
+    frames = max(a.steps, 1000)
+    flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(frames)]
+    clocks = Clocks(local)
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks.start()
+    with torch.cuda.stream(stream):
+        for f0, f1 in evs:
+            flush.fill_(1.0)
+            f0.record(stream)
+            render_sky(atm, draw, RENDER_W, RENDER_H, depth=depth, stream=stream)
+            f1.record(stream)
+    stream.synchronize()
+    clk = clocks.stop()
+    ms = max_over_ranks(world, sum(f0.elapsed_time(f1) for f0, f1 in evs)) / frames
+    pixels = RENDER_W * RENDER_H
+    from fuzzyblue_gb300.ranks import whole_job_rate
+    value = whole_job_rate(world, 1, ms / 1e3)
+    # end to end: depth in from pinned host memory, radiance out to it, every frame
+    depth_pin = torch.empty((RENDER_H, RENDER_W), dtype=torch.float32, pin_memory=True)
+    depth_pin.copy_(torch.from_numpy(depth_h))
+    out_pin = torch.empty((RENDER_H, RENDER_W, 4), dtype=torch.float32, pin_memory=True)
+    dev_depth = torch.empty((RENDER_H, RENDER_W), dtype=torch.float32, device="cuda")
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(frames):
+        with torch.cuda.stream(stream):
+            dev_depth.copy_(depth_pin, non_blocking=True)
+            color, _ = render_sky(atm, draw, RENDER_W, RENDER_H, depth=dev_depth, stream=stream)
+            out_pin.copy_(color, non_blocking=True)
+        stream.synchronize()
+    e2e_s = max_over_ranks(world, time.perf_counter() - t0) / frames
+    out = {
+        "metric": "frames/s, headless sky pass (radiance + transmittance) over the tables of one atmosphere",
+        "value": value, "unit": "frames/s", "n_gpus": world, "steps": frames, "warmup": max(a.warmup, 3),
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic: the default-size tables of atmosphere 0 of the uniform batch (seed 0), "
+                                "seeded depth buffer",
+        "config": {"workload": "sky pass, 1920x1080, half the pixels at finite depth (aerial perspective)",
+                   "width": RENDER_W, "height": RENDER_H, "pixels_per_s": value * pixels,
+                   "l2": "flushed between frames (256 MB written outside the timed events): cold tables "
+                         "(16.3 MB) and buffers every frame"},
+        "clocks": clk,
+        "e2e": {"value": whole_job_rate(world, 1, e2e_s), "unit": "frames/s",
+                "h2d_bytes_per_step": 4 * pixels, "d2h_bytes_per_step": 16 * pixels},
+        "gpu_launches": frames,
+        "roofline": {"bound": "hbm", "achieved": 36 * pixels / (ms / 1e3) / 1e9,
+                     "peak": measured_peaks().get("hbm_gbs"), "unit": "GB/s",
+                     "frac": (36 * pixels / (ms / 1e3) / 1e9) / measured_peaks()["hbm_gbs"]
+                     if measured_peaks().get("hbm_gbs") else None,
+                     "traffic": None,
+                     "note": "algorithmic bytes: the depth read and the radiance and transmittance written, "
+                             "36 B per pixel; the pass is bound by its table gathers (two 4D lookups of the "
+                             "scattering table and up to four transmittance lookups per pixel, L2-resident), "
+                             "not by HBM"},
+    }
+    if rank == 0 and not a.no_cpu_baseline:
+        from oracle import cpu_baseline as C
+        from oracle import py_oracle
+        t = atm.to_host()
+        w, h = RENDER_W // 8, RENDER_H // 8  # the same view at 1/64 of the pixels
+        dep = np.ascontiguousarray(depth_h[::8, ::8])
+        ref = C.reference_available()
+        t0 = time.perf_counter()
+        reps = 0
+        while reps < 3 or time.perf_counter() - t0 < 2.0:
+            py_oracle.render_sky(p, t["transmittance"], t["scattering"], draw, w, h, depth=dep, reference=ref)
+            reps += 1
+        sec = (time.perf_counter() - t0) / reps * (pixels / (w * h))
+        out["cpu_baseline"] = {"value": 1.0 / sec, "unit": "frames/s", "cores": os.cpu_count(),
+                               "kind": "reference" if ref else "port",
+                               "sample": "%dx%d frames of the same view, %d repetitions, scaled by the pixel count"
+                               % (w, h, reps)}
+    if rank == 0:
+        print(json.dumps(out))
+    atm.close()
+    builder.close()
+
+
 # ----------------------------------------------------------- uneven batch ---
 def run_uneven(a):
     """96 atmospheres (seed 1) split evenly over the default, half and double
@@ -698,6 +831,8 @@ def main():
         run_uneven(a)
     elif a.workload == "serve":
         run_serve(a)
+    elif a.workload == "render":
+        run_render(a)
     else:
         run_ours(a)
 
