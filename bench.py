@@ -653,6 +653,34 @@ def run_uneven(a):
     for p in params:
         c = "x".join(str(v) for v in p.scattering_extent())
         per_class[c] = per_class.get(c, 0) + 1
+    # batched vs plain per table class: each class's atmospheres as one batch,
+    # and the plain path, each atmosphere alone in FP32 (one call each)
+    from fuzzyblue_gb300.api import Atmosphere
+    compare = {}
+    plain_total = 0.0
+    for c in per_class:
+        members = [p for p in params if "x".join(str(v) for v in p.scattering_extent()) == c]
+        best = None
+        for _ in range(2):
+            t0 = time.perf_counter()
+            q = build_batch(builder, members, stream=stream)
+            q.wait()
+            q.release()
+            dt = time.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
+        plain = [p.replace(precision=PRECISION_PLAIN) for p in members]
+        w = Atmosphere.build(builder, plain[0], stream=stream)
+        w.wait()
+        w.release()
+        t0 = time.perf_counter()
+        for p in plain:
+            q = Atmosphere.build(builder, p, stream=stream)
+            q.wait()
+            q.release()
+        pt = time.perf_counter() - t0
+        plain_total += pt
+        compare[c] = {"atmospheres": len(members), "batched_atmospheres_per_s": len(members) / best,
+                      "plain_atmospheres_per_s": len(members) / pt, "batched_over_plain": pt / best}
     out = {
         "metric": "atmospheres/s, uneven batch of 96 over three table classes, orders 2-8, %s precision"
                   % a.precision,
@@ -668,6 +696,10 @@ def run_uneven(a):
         "e2e": {"value": 96 / e2e_s, "unit": "atmospheres/s", "h2d_bytes_per_step": 96 * 384,
                 "d2h_bytes_per_step": d2h // a.steps},
         "tile_shapes": tuned,
+        "plain": {"atmospheres_per_s": 96 / plain_total, "precision": "plain",
+                  "path": "each atmosphere alone, one call each, FP32"},
+        "batched_over_plain": (96 / (ms / 1e3)) / (96 / plain_total),
+        "per_class": compare,
     }
     print(json.dumps(out))
     builder.close()
