@@ -1405,6 +1405,9 @@ __global__ void __launch_bounds__(kDensThreads, V == 0 ? 4 : (V == 1 ? 3 : 5)) k
 // kMsWideThreads. The slab of a row holds the row plus a zero guard nu slice,
 // read with weight 0 where nu = 1 selects the last slice.
 constexpr int kMsMidThreads = 512;
+// Slab buffers of a tile: two samples are taken per barrier while the next two
+// are built.
+constexpr int kMsSlabs = 4;
 constexpr int kMsWideThreads = 1024;
 constexpr int kMsRowBytes = 96 * 1024;  // shared memory for the rows of a tile (records + slabs)
 struct MSShape {
@@ -1415,7 +1418,7 @@ struct MSShape {
 __host__ __device__ inline MSShape ms_shape(int W, int sc_mus, int steps, int threads) {
   MSShape m;
   m.slab_row = W + sc_mus + 1;
-  const int row_bytes = (int)sizeof(MSRec) * (steps + 1) + 2 * (int)sizeof(float4) * m.slab_row;
+  const int row_bytes = (int)sizeof(MSRec) * (steps + 1) + kMsSlabs * (int)sizeof(float4) * m.slab_row;
   m.R = W <= threads ? min(threads / W, max(1, kMsRowBytes / row_bytes)) : 1;
   m.TPT = (m.R * W + threads - 1) / threads;
   return m;
@@ -1435,7 +1438,7 @@ __host__ __device__ inline int tiles_multiple(int W, int sc_mus, int steps, int 
 }
 __host__ __device__ inline size_t ms_smem(int W, int steps, int sc_mus, int threads) {
   const MSShape m = ms_shape(W, sc_mus, steps, threads);
-  return align16(sizeof(MSRec) * (size_t)m.R * (steps + 1)) + 2 * sizeof(float4) * (size_t)m.R * m.slab_row;
+  return align16(sizeof(MSRec) * (size_t)m.R * (steps + 1)) + kMsSlabs * sizeof(float4) * (size_t)m.R * m.slab_row;
 }
 
 // Position t in [0, n - 1] within a row of n texels as (i0, f): texel i0 in
@@ -1468,7 +1471,7 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
   // selects the last slice) and one entry (read with weight 0 where the mu_s
   // position is the slice's last texel)
   const int ng = NM + 1;
-  for (int k = tid; k < 2 * nrow * ng; k += nth) {
+  for (int k = tid; k < kMsSlabs * nrow * ng; k += nth) {
     const int b = k / (nrow * ng), rem = k % (nrow * ng);
     slab[b * slab_stride + (rem / ng) * SR + W + rem % ng] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
@@ -1556,13 +1559,9 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
       }
     }
   };
-  load(0);
-  blend(0, slab);
-  __syncthreads();
   const float fmus = float(NM);
-  for (int i = 0; i < NS; ++i) {
-    const float4* cur = slab + (i & 1) * slab_stride;
-    if (kAhead && i + 1 < NS) load(i + 1);
+  // the texel work of sample i on its slab
+  auto step = [&](int i, const float4* cur) {
 #pragma unroll
     for (int j = 0; j < TPT; ++j) {
       if (tid + j * nth < nx_tex) {
@@ -1600,11 +1599,48 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
         }
       }
     }
-    if (i + 1 < NS) {
-      if (!kAhead) load(i + 1);
-      blend(i + 1, slab + ((i + 1) & 1) * slab_stride);
+  };
+  auto slab_of = [&](int i) { return slab + (i % kMsSlabs) * slab_stride; };
+  if (MX) {
+    // two samples per barrier: i and i + 1 from their slabs while i + 2 and
+    // i + 3 are built (measured faster for the mixed kernels; the plain ones
+    // run faster one sample per barrier)
+    load(0);
+    blend(0, slab_of(0));
+    if (NS > 1) {
+      load(1);
+      blend(1, slab_of(1));
     }
     __syncthreads();
+    for (int i = 0; i < NS; i += 2) {
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int k = i + h;
+        if (k < NS) {
+          if (kAhead && k + 2 < NS) load(k + 2);
+          step(k, slab_of(k));
+          if (k + 2 < NS) {
+            if (!kAhead) load(k + 2);
+            blend(k + 2, slab_of(k + 2));
+          }
+        }
+      }
+      __syncthreads();
+    }
+  } else {
+    // one sample per barrier: i from its slab while i + 1 is built
+    load(0);
+    blend(0, slab_of(0));
+    __syncthreads();
+    for (int i = 0; i < NS; ++i) {
+      if (kAhead && i + 1 < NS) load(i + 1);
+      step(i, slab_of(i));
+      if (i + 1 < NS) {
+        if (!kAhead) load(i + 1);
+        blend(i + 1, slab_of(i + 1));
+      }
+      __syncthreads();
+    }
   }
   // outputs: delta multiple scattering and the final table (:91-92)
 #pragma unroll
