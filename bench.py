@@ -350,6 +350,17 @@ def run_ours(a):
     ref_achieved = ref_flops / (dens_ms / 1e3) / 1e12
     traffic = profile_value(LAUNCH_PROFILE, "dram_bytes_per_launch_order3")
     peaks = measured_peaks()
+    # the launch's binding limit is instruction issue: warp instructions per
+    # launch (ncu's thread instructions per direction / 32) against one per
+    # cycle per scheduler, 4 schedulers per SM
+    instr_per_dir = profile_value(DENSITY_PROFILE, "thread_instr_per_direction_order3")
+    issue = None
+    if instr_per_dir:
+        issue_achieved = directions * instr_per_dir / 32.0 / (dens_ms / 1e3) / 1e9
+        issue_peak = sms * 4 * mhz * 1e6 / 1e9
+        issue = {"achieved": issue_achieved, "peak": issue_peak, "unit": "G warp instructions/s",
+                 "frac": issue_achieved / issue_peak, "thread_instr_per_unit": instr_per_dir,
+                 "source": "thread instructions per direction, ncu, profiles/" + DENSITY_PROFILE}
 
     out = {
         "metric": METRIC if a.precision == "mixed" else METRIC.replace(
@@ -387,6 +398,7 @@ def run_ours(a):
                      "traffic": traffic, "traffic_source": "ncu DRAM bytes of the same launch, profiles/" + LAUNCH_PROFILE,
                      "hbm": {"achieved_gbs": traffic / (dens_ms / 1e3) / 1e9 if traffic else None,
                              "peak_gbs": peaks.get("hbm_gbs"), "peak_source": "MEASURED_PEAKS.json"},
+                     "issue": issue,
                      "reference_algorithm": {
                          "achieved": ref_achieved, "frac": ref_achieved / peak,
                          "flop_per_texel": FLOP_PER_TEXEL["density_order3"],
