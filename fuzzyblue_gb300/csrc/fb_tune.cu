@@ -100,18 +100,17 @@ extern "C" int fb_builder_autotune(fb_builder* b, const fb_params* classes, uint
           fbi::tuning_set(fbi::builder_tuning(b), t);
         }
         const float ms = time_launch(b, batchv, FB_KERNEL_DENSITY, 3, 2);
-        if (ms < 0) {
-          status = fbi::set_error(FB_ERR_CUDA, "autotune build failed");
-          break;
-        }
+        if (ms < 0) continue;  // a candidate that cannot launch here (e.g. its shared memory) is skipped
         if (best.dens_ms < 0 || ms < best.dens_ms) {
           best = t;
           best.dens_ms = ms;
         }
       }
-      if (status != FB_OK) break;
     }
-    if (status != FB_OK) break;
+    if (best.dens_ms < 0) {
+      status = fbi::set_error(FB_ERR_CUDA, "autotune: no density candidate could be built");
+      break;
+    }
     best.ms_ms = -1.0f;
     for (int v = 0; v < 2; ++v) {
       fbi::TuneEntry t = best;
@@ -121,10 +120,7 @@ extern "C" int fb_builder_autotune(fb_builder* b, const fb_params* classes, uint
         fbi::tuning_set(fbi::builder_tuning(b), t);
       }
       const float ms = time_launch(b, batchv, FB_KERNEL_MULTIPLE, 3, 2);
-      if (ms < 0) {
-        status = fbi::set_error(FB_ERR_CUDA, "autotune build failed");
-        break;
-      }
+      if (ms < 0) continue;
       if (best.ms_ms < 0 || ms < best.ms_ms) {
         best.ms_variant = v;
         best.ms_ms = ms;
