@@ -778,7 +778,7 @@ def run_serve(a):
             arrivals.append(t)
         reqs = [workloads.serving_request(rng, precision=prec) for _ in arrivals]
         srv = Server(builder, hbm_budget_bytes=120 * 10 ** 9, max_queue=a.max_queue)
-        submit_at, done_at, rejected, fresh, cls_at = {}, {}, [0], [], {}
+        submit_at, done_at, rejected, cls_at = {}, {}, [0], {}
         lock = threading.Lock()
         start = time.perf_counter() + 0.05
 
@@ -796,35 +796,35 @@ def run_serve(a):
                 with lock:
                     submit_at[tk] = start + at
                     cls_at[tk] = cls_of(p)
-                    fresh.append(tk)
         th = threading.Thread(target=submitter)
         th.start()
-        outstanding = []
+        # finished tickets come from the server's completion queue
+        # (fb_server_completed): one call per wake-up, not a poll per ticket
+        failed = [0]
         deadline = start + a.duration + 120.0
         while time.perf_counter() < deadline:
-            with lock:
-                outstanding.extend(fresh)
-                fresh.clear()
-            still = []
-            for tk in outstanding:
-                if srv.poll(tk) is not None:
-                    done_at[tk] = time.perf_counter()
-                    srv.release(tk)
+            for tk in srv.completed(timeout_ms=1):
+                now = time.perf_counter()
+                try:
+                    ok = srv.poll(tk) is not None
+                except N.FuzzyblueError:
+                    ok = False
+                if ok:
+                    done_at[tk] = now
                 else:
-                    still.append(tk)
-            outstanding = still
-            if not th.is_alive() and not outstanding:
+                    failed[0] += 1
+                srv.release(tk)
+            if not th.is_alive():
                 with lock:
-                    if not fresh:
+                    if len(done_at) + failed[0] >= len(submit_at):
                         break
-            time.sleep(0.0005)
         th.join()
         st = srv.stats()
         srv.close()
         lat = np.array([done_at[k] - submit_at[k] for k in done_at]) * 1e3
         lat_cls = {c: np.array([done_at[k] - submit_at[k] for k in done_at if cls_at[k] == c]) * 1e3 for c in names}
         end = max(done_at.values()) if done_at else start
-        served = {"completed": len(done_at), "rejected": rejected[0],
+        served = {"completed": len(done_at), "rejected": rejected[0], "failed": failed[0],
                   "throughput": len(done_at) / max(end - start, 1e-9),
                   "p50_ms": float(np.percentile(lat, 50)) if len(lat) else None,
                   "p99_ms": float(np.percentile(lat, 99)) if len(lat) else None,

@@ -164,6 +164,7 @@ SIGNATURES = {
     "fb_server_poll": (_I, [_V, _U64, ctypes.POINTER(_V)]),
     "fb_server_wait": (_I, [_V, _U64, _U32, ctypes.POINTER(_V)]),
     "fb_server_release": (_I, [_V, _U64]),
+    "fb_server_completed": (_I, [_V, ctypes.POINTER(_U64), _U32, _U32, ctypes.POINTER(_U32)]),
     "fb_server_cancel": (_I, [_V, _U64]),
     "fb_server_get_stats": (_I, [_V, ctypes.POINTER(c_server_stats)]),
     "fb_server_destroy": (None, [_V]),

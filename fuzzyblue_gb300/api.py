@@ -383,6 +383,15 @@ class Server:
         N.check(N.lib().fb_server_release(self._h, ticket), "fb_server_release")
         self._params.pop(ticket, None)
 
+    def completed(self, timeout_ms: int = 0, capacity: int = 4096) -> List[int]:
+        """Tickets that finished (ready or failed) since earlier calls, oldest
+        first (fb_server_completed); waits up to timeout_ms for the first."""
+        buf = (ctypes.c_uint64 * capacity)()
+        n = ctypes.c_uint32()
+        N.check(N.lib().fb_server_completed(self._h, buf, capacity, timeout_ms, ctypes.byref(n)),
+                "fb_server_completed")
+        return list(buf[:n.value])
+
     def cancel(self, ticket: int) -> bool:
         """True if the request was cancelled before it started."""
         return N.check(N.lib().fb_server_cancel(self._h, ticket), "fb_server_cancel") == N.FB_OK

@@ -103,6 +103,7 @@ struct fb_server {
   std::thread th;
   bool stop = false;
   std::deque<uint64_t> queue;
+  std::deque<uint64_t> finished;  // tickets completed or failed, not yet taken by fb_server_completed
   std::unordered_map<uint64_t, Request> reqs;
   std::unordered_map<std::string, Entry*> entries;
   std::vector<Batch*> inflight;
@@ -131,6 +132,8 @@ void complete_request(fb_server* s, uint64_t t, Entry* e) {
   r.t_done = now_ms();
   s->lat.push_back(r.t_done - r.t_submit);
   s->st.completed++;
+  s->finished.push_back(t);
+  s->cv_done.notify_all();
 }
 
 void fail_request(fb_server* s, uint64_t t, int status) {
@@ -138,6 +141,8 @@ void fail_request(fb_server* s, uint64_t t, int status) {
   if (it == s->reqs.end()) return;
   it->second.state = State::Failed;
   it->second.status = status;
+  s->finished.push_back(t);
+  s->cv_done.notify_all();
 }
 
 // Frees unpinned resident tables, least recently used first, until `need`
@@ -566,6 +571,27 @@ extern "C" int fb_server_wait(fb_server* s, uint64_t t, uint32_t timeout_ms, fb_
   }
 }
 
+extern "C" int fb_server_completed(fb_server* s, uint64_t* tickets, uint32_t capacity, uint32_t timeout_ms,
+                                   uint32_t* count) {
+  if (!s || !count || (!tickets && capacity)) return fail_srv(FB_ERR_INVALID_ARGUMENT, "NULL argument");
+  std::unique_lock<std::mutex> g(s->mu);
+  if (s->finished.empty() && timeout_ms) {
+    auto ready = [&] { return !s->finished.empty() || s->stop; };
+    if (timeout_ms == UINT32_MAX) {
+      s->cv_done.wait(g, ready);
+    } else {
+      s->cv_done.wait_until(g, std::chrono::steady_clock::now() + std::chrono::milliseconds(timeout_ms), ready);
+    }
+  }
+  uint32_t n = 0;
+  while (n < capacity && !s->finished.empty()) {
+    tickets[n++] = s->finished.front();
+    s->finished.pop_front();
+  }
+  *count = n;
+  return FB_OK;
+}
+
 extern "C" int fb_server_release(fb_server* s, uint64_t t) {
   if (!s) return fail_srv(FB_ERR_INVALID_ARGUMENT, "server is NULL");
   std::lock_guard<std::mutex> g(s->mu);
@@ -632,6 +658,7 @@ extern "C" void fb_server_destroy(fb_server* s) {
     s->queue.clear();
   }
   s->cv.notify_all();
+  s->cv_done.notify_all();
   if (s->th.joinable()) s->th.join();
   cudaSetDevice(fbi::builder_device(s->b));
   for (auto& kv : s->entries) {

@@ -358,6 +358,14 @@ int fb_server_submit(fb_server* s, const fb_params* p, uint64_t* ticket);
 int fb_server_poll(fb_server* s, uint64_t ticket, fb_atmosphere** out);
 /* As fb_server_poll, blocking up to timeout_ms (UINT32_MAX: no limit). */
 int fb_server_wait(fb_server* s, uint64_t ticket, uint32_t timeout_ms, fb_atmosphere** out);
+/* Copies into `tickets` up to `capacity` tickets of requests that finished
+ * (ready or failed) since earlier calls, oldest first, and sets *count; the
+ * rest stay for the next call. With none waiting it blocks up to timeout_ms
+ * (0: return at once, UINT32_MAX: until one finishes or the server stops).
+ * One call replaces polling every outstanding ticket; fb_server_poll then
+ * gives each ticket's tables or status. */
+int fb_server_completed(fb_server* s, uint64_t* tickets, uint32_t capacity, uint32_t timeout_ms,
+                        uint32_t* count);
 /* The caller is done with the ticket's tables; they may now be evicted. */
 int fb_server_release(fb_server* s, uint64_t ticket);
 /* Cancels a request that has not started; FB_NOT_READY if it is running. */

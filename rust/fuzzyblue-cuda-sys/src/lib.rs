@@ -263,6 +263,8 @@ extern "C" {
     pub fn fb_server_poll(s: *mut fb_server, ticket: u64, out: *mut *mut fb_atmosphere) -> c_int;
     pub fn fb_server_wait(s: *mut fb_server, ticket: u64, timeout_ms: u32, out: *mut *mut fb_atmosphere) -> c_int;
     pub fn fb_server_release(s: *mut fb_server, ticket: u64) -> c_int;
+    pub fn fb_server_completed(s: *mut fb_server, tickets: *mut u64, capacity: u32, timeout_ms: u32,
+                               count: *mut u32) -> c_int;
     pub fn fb_server_cancel(s: *mut fb_server, ticket: u64) -> c_int;
     pub fn fb_server_get_stats(s: *mut fb_server, out: *mut fb_server_stats) -> c_int;
     pub fn fb_server_destroy(s: *mut fb_server);

@@ -125,3 +125,22 @@ def test_cancel_queued_request(builder):
             assert srv.stats()["cancelled"] == 1
         else:  # it had already started: it completes normally
             assert srv.wait(t1, 60000) is not None
+
+
+def test_completion_queue_lists_every_finished_ticket_once(builder):
+    """fb_server_completed: every submitted ticket, cache hits included, comes
+    out of the completion queue exactly once; polling it then gives its tables."""
+    from fuzzyblue_gb300.api import Server
+    ps = _mix()
+    ps.append(ps[0])  # identical to the first: shared with its build or resident
+    with Server(builder, max_batch=3, max_inflight=3) as srv:
+        tickets = [srv.submit(p) for p in ps]
+        seen = []
+        t0 = time.perf_counter()
+        while len(seen) < len(tickets) and time.perf_counter() - t0 < 120:
+            seen.extend(srv.completed(timeout_ms=100))
+        assert sorted(seen) == sorted(tickets)
+        assert srv.completed(timeout_ms=0) == []
+        for t in tickets:
+            assert srv.poll(t) is not None
+            srv.release(t)
