@@ -203,7 +203,6 @@ __device__ __forceinline__ Axis bounded_axis(Axis a, int n) {
 }
 
 __device__ __forceinline__ float4 ld4(const float4* p) { return __ldg(p); }
-__device__ __forceinline__ float3 f3(float4 v) { return make_float3(v.x, v.y, v.z); }
 
 // Bilinear RGB fetch with the Vulkan weight order (1-a)(1-b), a(1-b), (1-a)b, ab.
 __device__ __forceinline__ float3 fetch2(const float4* t, int w, Axis x, Axis y) {
@@ -652,14 +651,6 @@ __device__ __forceinline__ float clamp_nu32(float nu_raw, float mu, float mu_s, 
   float sq = sqrtf((1.0f - mu * mu) * one_m_mus2);
   return gclamp(nu_raw, mu * mu_s - sq, mu * mu_s + sq);
 }
-__device__ __forceinline__ void decode_texel32(const DevAtmo& a, const Geo32& G, uint32_t ix, uint32_t iy,
-                                               uint32_t iz, float& r, float& mu, float& mu_s, float& nu,
-                                               bool& ground) {
-  decode_yz32(a, G, iy, iz, r, mu, ground);
-  float nu_raw;
-  decode_x32(a, G, ix, mu_s, nu_raw);
-  nu = clamp_nu32(nu_raw, mu, mu_s, 1.0f - mu_s * mu_s);
-}
 
 // MIXED: the same decode in FP64, producing q and s directly.
 __device__ __forceinline__ void decode_yz64(const DevAtmo& a, const Geo64& G, uint32_t iy, uint32_t iz,
@@ -699,15 +690,4 @@ __device__ __forceinline__ void decode_x64(const DevAtmo& a, const Geo64& G, uin
   mu_s = d == 0.0 ? 1.0 : clamp_cosine((G.H2 - d * d) / (2.0 * G.R * d));
   nu_raw = clamp_cosine(f_nu / double(a.sc_nu - 1) * 2.0 - 1.0);
 }
-__device__ __forceinline__ TexelParams decode_texel64(const DevAtmo& a, const Geo64& G, uint32_t ix, uint32_t iy,
-                                                      uint32_t iz) {
-  TexelParams o;
-  decode_yz64(a, G, iy, iz, o);
-  double nu;
-  decode_x64(a, G, ix, o.mu_s, nu);
-  double sq = sqrt((1.0 - o.mu * o.mu) * (1.0 - o.mu_s * o.mu_s));
-  o.nu = gclamp(nu, o.mu * o.mu_s - sq, o.mu * o.mu_s + sq);
-  return o;
-}
-
 }  // namespace fb
