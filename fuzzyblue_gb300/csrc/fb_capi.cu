@@ -594,7 +594,10 @@ void plan_group(Plan& P, const std::vector<DevAtmo>& A, const std::vector<int>& 
       if (A[j].order >= n) jobs.push_back(j);
     PlannedLaunch D = mk(fb::kPassDensity, n);
     std::vector<int> t0, t1;
-    bool cl = false;
+    // the tuned variant (occupancy, + kDensClamped for exact-size tables); the
+    // exact-size tables also wherever the power-of-two ones do not fit
+    const int tuned = launch_variant(A, jobs, tun, mixed, true);
+    bool cl = tuned >= fb::kDensClamped;
     for (int j : jobs) cl |= fb::density_smem(A[j], n == 2, mixed, false) > smem_limit;
     for (int j : jobs) {
       const DevAtmo& a = A[j];
@@ -607,7 +610,7 @@ void plan_group(Plan& P, const std::vector<DevAtmo>& A, const std::vector<int>& 
     add_segment(P, D, 0, jobs, t0);
     add_segment(P, D, 1, jobs, t1);
     D.nseg = 2;
-    D.variant = launch_variant(A, jobs, tun, mixed, true) + (cl ? fb::kDensClamped : 0);
+    D.variant = tuned % fb::kDensClamped + (cl ? fb::kDensClamped : 0);
     P.launches.push_back(D);
     PlannedLaunch M = mk(fb::kPassMultiple, n);
     std::vector<int> tm;

@@ -4,8 +4,9 @@
 // batch of that class at order 3 with per-launch timing events, once per
 // candidate: every valid scattering-density tile shape (mu_s columns x mu
 // rows per 128-thread block) in the three occupancy variants of the density
-// kernel (4, 3 or 5 resident blocks per SM), then both variants of the
-// multiple-scattering kernel. The fastest of each is
+// kernel (4, 3 or 5 resident blocks per SM), each with power-of-two and with
+// exact-size interval tables, then both variants of the multiple-scattering
+// kernel. The fastest of each is
 // kept in the builder's tuning table, which every later build consults.
 #include <cuda_runtime.h>
 
@@ -90,7 +91,7 @@ extern "C" int fb_builder_autotune(fb_builder* b, const fb_params* classes, uint
     fbi::TuneEntry best = e;
     best.dens_ms = -1.0f;
     for (const Cand& cd : density_candidates(p)) {
-      for (int v = 0; v < 3; ++v) {
+      for (int v = 0; v < 2 * fb::kDensClamped; ++v) {  // occupancy variants, power-of-two and exact-size tables
         fbi::TuneEntry t = e;
         t.dens_S = cd.S;
         t.dens_chunk = cd.chunk;
@@ -220,7 +221,7 @@ extern "C" int fb_builder_load_tuning(fb_builder* b, const char* path) {
     e.precision = (int)v[4];
     e.dens_S = (int)v[5];
     e.dens_chunk = (int)v[6];
-    e.dens_variant = std::min(2, std::max(0, (int)v[7]));
+    e.dens_variant = std::min(2 * fb::kDensClamped - 1, std::max(0, (int)v[7]));
     e.ms_variant = std::min(1, std::max(0, (int)v[8]));
     e.dens_ms = (float)v[9];
     e.ms_ms = (float)v[10];

@@ -290,7 +290,8 @@ int fb_batch_build(fb_builder* b, void* stream, const fb_params* params,
 typedef struct fb_tile_shape {
     uint32_t density_columns;  /* mu_s columns per scattering-density tile */
     uint32_t density_rows;     /* mu rows per scattering-density tile */
-    uint32_t density_variant;  /* density kernel occupancy: 0, 1, 2 = 4, 3, 5 blocks per SM */
+    uint32_t density_variant;  /* density kernel: 0, 1, 2 = registers for 4, 3, 5 blocks per SM;
+                                  3-5: the same with exact-size interval tables */
     uint32_t multiple_variant; /* occupancy variant of the multiple-scattering kernel */
     float density_ms;          /* measured time of the chosen density launch */
     float multiple_ms;         /* measured time of the chosen multiple-scattering launch */
