@@ -1401,9 +1401,11 @@ __global__ void __launch_bounds__(kDensThreads, V == 0 ? 4 : (V == 1 ? 3 : 5)) k
 // per CTA for rows of at most `threads` texels, else one row with TPT texels
 // per thread. Launches use CTAs of kThreads threads; when a row of the launch
 // is wider, CTAs of kMsMidThreads (two per SM, so that one runs while the
-// other waits at its per-sample barrier) up to rows of 1024 texels, else of
-// kMsWideThreads. The slab of a row holds the row plus a zero guard nu slice,
-// read with weight 0 where nu = 1 selects the last slice.
+// other waits at its per-sample barrier) up to rows of 512 texels, else of
+// kMsWideThreads (one texel per thread up to rows of 1024: measured faster
+// than two per thread on kMsMidThreads, which spill). The slab of a row holds
+// the row plus a zero guard nu slice, read with weight 0 where nu = 1 selects
+// the last slice.
 constexpr int kMsMidThreads = 512;
 // Slab buffers of a tile: two samples are taken per barrier while the next two
 // are built.
@@ -1425,7 +1427,7 @@ __host__ __device__ inline MSShape ms_shape(int W, int sc_mus, int steps, int th
 }
 // CTA size of a launch over rows of width W (the widest of the launch).
 __host__ __device__ inline int ms_threads(int W) {
-  return W <= kThreads ? kThreads : (W <= 2 * kMsMidThreads ? kMsMidThreads : kMsWideThreads);
+  return W <= kThreads ? kThreads : (W <= kMsMidThreads ? kMsMidThreads : kMsWideThreads);
 }
 // Kernel variant of a launch of `block` threads: 2 and 3 for the wide CTA
 // sizes, -1 for kThreads (the tuned occupancy variant 0 or 1 applies).
