@@ -55,6 +55,7 @@ class c_intermediates(ctypes.Structure):
         ("delta_mie", ctypes.c_void_p),
         ("delta_multiple_scattering", ctypes.c_void_p),
         ("scattering_density", ctypes.c_void_p),
+        ("scattering_density_stride", ctypes.c_uint32),
     ]
 
 

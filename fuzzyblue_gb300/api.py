@@ -49,6 +49,23 @@ class DeviceArray:
         return t.cpu().numpy()
 
 
+class PlanarDensity(DeviceArray):
+    """The scattering-density temporary, stored as three float planes (R, G, B)
+    per (r, mu) row of `stride` floats; to_numpy() gives the RGBA layout of the
+    other scattering-class tables (alpha 0, as scattering_density.comp:155 writes)."""
+
+    def __init__(self, ptr: int, extent, stride: int, owner=None):
+        sd, sh, sw = extent
+        super().__init__(ptr, (sd, sh, 3, int(stride)), owner)
+        self.width = int(sw)
+
+    def to_numpy(self) -> np.ndarray:
+        planes = super().to_numpy()[..., :self.width]
+        out = np.zeros(planes.shape[:2] + (self.width, 4), np.float32)
+        out[..., :3] = np.moveaxis(planes, 2, 3)
+        return out
+
+
 class Builder:
     """Builder::new (src/precompute.rs:61-68): one CUDA device and its kernels."""
 
@@ -293,7 +310,7 @@ class PendingAtmosphere:
             "delta_rayleigh": DeviceArray(m.delta_rayleigh, sc, self),
             "delta_mie": DeviceArray(m.delta_mie, sc, self),
             "delta_multiple_scattering": DeviceArray(m.delta_multiple_scattering, sc, self),
-            "scattering_density": DeviceArray(m.scattering_density, sc, self),
+            "scattering_density": PlanarDensity(m.scattering_density, (sd, sh, sw), m.scattering_density_stride, self),
         }
 
     def profile(self) -> List[dict]:

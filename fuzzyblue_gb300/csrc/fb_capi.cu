@@ -193,7 +193,9 @@ TableSizes sizes_of(const fb_params& p) {
   s.nir = (size_t)r.irradiance_mu_s_size * r.irradiance_r_size;
   s.nsc = (size_t)r.scattering_nu_size * r.scattering_mu_s_size * r.scattering_mu_size * r.scattering_r_size;
   s.out_bytes = align256(16 * s.ntr) + align256(16 * s.nir) + align256(16 * s.nsc);
-  s.tmp_bytes = 2 * align256(16 * s.nir) + 4 * align256(16 * s.nsc);
+  const size_t rows = (size_t)r.scattering_mu_size * r.scattering_r_size;
+  s.dens_bytes = 12 * rows * (size_t)fb::dens_stride((int)(r.scattering_nu_size * r.scattering_mu_s_size));
+  s.tmp_bytes = 2 * align256(16 * s.nir) + 3 * align256(16 * s.nsc) + align256(s.dens_bytes);
   if (p.precision == FB_PRECISION_MIXED) s.tmp_bytes += align256(24 * s.nsc) + align256(24 * s.nir);
   s.tmp_bytes += geometry_bytes(p);
   return s;
@@ -669,6 +671,7 @@ void fill_devatmo(DevAtmo& d, const fb_params& p, const fbi::Tuning& tun) {
   d.order = (int)p.order;
   d.f16 = p.storage == FB_STORAGE_F16;
   d.W = d.sc_nu * d.sc_mus;
+  d.Wd = fb::dens_stride(d.W);
   {
     const double R = d.bottom, T = d.top;
     d.H2d = T * T - R * R;
@@ -756,7 +759,7 @@ int build(fb_builder* b, cudaStream_t s, const fb_params* params, uint32_t count
     d.dr = (float4*)tp;      tp += align256(16 * z.nsc);
     d.dm = (float4*)tp;      tp += align256(16 * z.nsc);
     d.dms = (float4*)tp;     tp += align256(16 * z.nsc);
-    d.dens = (float4*)tp;    tp += align256(16 * z.nsc);
+    d.dens = (float*)tp;     tp += align256(z.dens_bytes);
     if (params[i].precision == FB_PRECISION_MIXED) {
       d.sc_acc = (double*)tp; tp += align256(24 * z.nsc);
       d.ir_acc = (double*)tp; tp += align256(24 * z.nir);
@@ -962,6 +965,7 @@ extern "C" int fb_pending_intermediates(fb_pending* p, uint32_t i, fb_intermedia
   o->delta_mie = d.dm;
   o->delta_multiple_scattering = d.dms;
   o->scattering_density = d.dens;
+  o->scattering_density_stride = (uint32_t)d.Wd;
   return FB_OK;
 }
 

@@ -42,6 +42,9 @@ struct RowGeo {
   int ground, pad;
 };
 
+// Plane stride of the density table, so that every plane row starts 16-byte aligned.
+__host__ __device__ inline int dens_stride(int W) { return (W + 3) & ~3; }
+
 // One x column of the packed table (nu slice x / mu_s_size, mu_s index x % mu_s_size).
 struct ColGeo {
   float mu_s, one_m_mus2, nu_raw, u_mus;  // PLAIN: reference float values; u_mus = u_mu_s texture coordinate
@@ -50,7 +53,7 @@ struct ColGeo {
 
 // One trapezoid sample of multiple scattering along the view ray of a row:
 // distance, 1/r_i, transmittance x dx x trapezoid weight; the bilinear
-// weights and element offsets ((z sc_mu + y) W) of the four density rows
+// weights and 16-byte offsets ((z sc_mu + y) 3 Wd / 4) of the four density rows
 // around the sample's (mu, r), corners (y0, z0), (y1, z0), (y0, z1), (y1, z1).
 struct __align__(16) MSRec {
   float d, inv_r, tvwx, tvwy;
@@ -96,6 +99,7 @@ struct DevAtmo {
   int tr_steps, ss_steps, ms_steps, dens_n, irr_n, order;
   int f16;         // round the scattering-class tables to half on store
   int W;           // sc_nu * sc_mus, width of the packed 3D scattering tables
+  int Wd;          // plane stride of the density table: W rounded up to a multiple of 4
   int dens_S, dens_chunk;  // scattering-density tile shape (0 = default; set by the autotuner)
   // Per-atmosphere constants of the MIXED geometry, computed on the host in
   // FP64 (correctly rounded, the values the device would compute) so that no
@@ -113,7 +117,8 @@ struct DevAtmo {
   float4* dr;       // delta Rayleigh (single)
   float4* dm;       // delta Mie (single)
   float4* dms;      // delta multiple scattering of the last order
-  float4* dens;     // scattering density of the current order
+  float* dens;      // scattering density of the current order: per (r, mu) row three
+                    // planes (R, G, B) of Wd floats, the first W of each in use
   double* sc_acc;   // MIXED: FP64 running sum of scattering rgb (3 per texel)
   double* ir_acc;   // MIXED: FP64 running sum of irradiance rgb (3 per texel)
   // geometry tables (written by the transmittance and single-scattering launches)

@@ -11,6 +11,7 @@ namespace fbi {
 
 struct TableSizes {
   size_t ntr, nir, nsc;   // texels
+  size_t dens_bytes;      // the planar scattering-density table
   size_t out_bytes;       // transmittance + irradiance + scattering
   size_t tmp_bytes;       // temporaries of one build
 };

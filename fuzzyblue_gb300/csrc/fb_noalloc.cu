@@ -150,7 +150,7 @@ extern "C" int fb_atmosphere_build_noalloc(void* stream, const fb_params* p, voi
   d.dr = (float4*)tp;      tp += align256(16 * z.nsc);
   d.dm = (float4*)tp;      tp += align256(16 * z.nsc);
   d.dms = (float4*)tp;     tp += align256(16 * z.nsc);
-  d.dens = (float4*)tp;    tp += align256(16 * z.nsc);
+  d.dens = (float*)tp;     tp += align256(z.dens_bytes);
   if (mixed) {
     d.sc_acc = (double*)tp; tp += align256(24 * z.nsc);
     d.ir_acc = (double*)tp; tp += align256(24 * z.nir);

@@ -431,10 +431,11 @@ template <bool MX> __device__ void tile_msrec(const DevAtmo& a, int tile) {
   o.w[1] = ay.f * (1.f - az.f);
   o.w[2] = (1.f - ay.f) * az.f;
   o.w[3] = ay.f * az.f;
-  o.off[0] = (az.i0 * a.sc_mu + ay.i0) * a.W;
-  o.off[1] = (az.i0 * a.sc_mu + ay.i1) * a.W;
-  o.off[2] = (az.i1 * a.sc_mu + ay.i0) * a.W;
-  o.off[3] = (az.i1 * a.sc_mu + ay.i1) * a.W;
+  const int rs = 3 * a.Wd / 4;  // float4s per density row
+  o.off[0] = (az.i0 * a.sc_mu + ay.i0) * rs;
+  o.off[1] = (az.i0 * a.sc_mu + ay.i1) * rs;
+  o.off[2] = (az.i1 * a.sc_mu + ay.i0) * rs;
+  o.off[3] = (az.i1 * a.sc_mu + ay.i1) * rs;
   a.g_ms[k] = o;
 }
 
@@ -1221,13 +1222,15 @@ __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned cha
     for (int j = 0; j < kDensMaxGroup; ++j) {
       if (j < G) {
         const int x = (grp * G + j) * a.sc_mus + si;
-        const size_t tt = ((size_t)zi * a.sc_mu + y) * a.W + x;
+        float* row = a.dens + ((size_t)zi * a.sc_mu + y) * 3 * a.Wd;
         float3 o = acc[j];
         if (MX)
           o = make_float3(accs[(6 * j) * kDensThreads] - accs[(6 * j + 3) * kDensThreads],
                           accs[(6 * j + 1) * kDensThreads] - accs[(6 * j + 4) * kDensThreads],
                           accs[(6 * j + 2) * kDensThreads] - accs[(6 * j + 5) * kDensThreads]);
-        a.dens[tt] = store_round4(make_float4(o.x, o.y, o.z, 0.f), a.f16);
+        row[x] = store_round(o.x, a.f16);
+        row[a.Wd + x] = store_round(o.y, a.f16);
+        row[2 * a.Wd + x] = store_round(o.z, a.f16);
       }
     }
   }
@@ -1403,9 +1406,11 @@ __global__ void __launch_bounds__(kDensThreads, V == 0 ? 4 : (V == 1 ? 3 : 5)) k
 // is wider, CTAs of kMsMidThreads (two per SM, so that one runs while the
 // other waits at its per-sample barrier) up to rows of 512 texels, else of
 // kMsWideThreads (one texel per thread up to rows of 1024: measured faster
-// than two per thread on kMsMidThreads, which spill). The slab of a row holds
-// the row plus a zero guard nu slice, read with weight 0 where nu = 1 selects
-// the last slice.
+// than two per thread on kMsMidThreads, which spill). The slab of a row holds,
+// like the density table, three planes (R, G, B): each the row plus a zero
+// guard nu slice, read with weight 0 where nu = 1 selects the last slice. A
+// thread builds four entries of one plane from four 16-byte loads (one per
+// density row), so the unused fourth channel of an RGBA table is never moved.
 constexpr int kMsMidThreads = 512;
 // Slab buffers of a tile: two samples are taken per barrier while the next two
 // are built.
@@ -1415,12 +1420,12 @@ constexpr int kMsRowBytes = 96 * 1024;  // shared memory for the rows of a tile 
 struct MSShape {
   int R;         // rows per tile
   int TPT;       // texels per thread
-  int slab_row;  // slab entries per row: W, a zero guard slice and one zero entry
+  int slab_row;  // floats per slab plane: W, a zero guard slice and one zero entry, rounded up to 4
 };
 __host__ __device__ inline MSShape ms_shape(int W, int sc_mus, int steps, int threads) {
   MSShape m;
-  m.slab_row = W + sc_mus + 1;
-  const int row_bytes = (int)sizeof(MSRec) * (steps + 1) + kMsSlabs * (int)sizeof(float4) * m.slab_row;
+  m.slab_row = (W + sc_mus + 1 + 3) & ~3;
+  const int row_bytes = (int)sizeof(MSRec) * (steps + 1) + kMsSlabs * 3 * (int)sizeof(float) * m.slab_row;
   m.R = W <= threads ? min(threads / W, max(1, kMsRowBytes / row_bytes)) : 1;
   m.TPT = (m.R * W + threads - 1) / threads;
   return m;
@@ -1440,7 +1445,7 @@ __host__ __device__ inline int tiles_multiple(int W, int sc_mus, int steps, int 
 }
 __host__ __device__ inline size_t ms_smem(int W, int steps, int sc_mus, int threads) {
   const MSShape m = ms_shape(W, sc_mus, steps, threads);
-  return align16(sizeof(MSRec) * (size_t)m.R * (steps + 1)) + kMsSlabs * sizeof(float4) * (size_t)m.R * m.slab_row;
+  return align16(sizeof(MSRec) * (size_t)m.R * (steps + 1)) + kMsSlabs * 3 * sizeof(float) * (size_t)m.R * m.slab_row;
 }
 
 // Position t in [0, n - 1] within a row of n texels as (i0, f): texel i0 in
@@ -1464,25 +1469,25 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
   const int nrow = min(sh.R, nrows - row0);
   const int N = a.ms_steps, NS = N + 1;
   const int tid = threadIdx.x;
-  const int SR = sh.slab_row;                      // slab stride per row
+  const int SR = sh.slab_row;                      // slab plane stride
   MSRec* rec = (MSRec*)smem;
-  float4* slab = (float4*)(smem + align16(sizeof(MSRec) * (size_t)sh.R * NS));
+  float* slab = (float*)(smem + align16(sizeof(MSRec) * (size_t)sh.R * NS));
   const int nx_tex = nrow * W;                     // texels of the tile = slab entries built per sample
-  const int slab_stride = sh.R * SR;
-  // zero guard after each row: a nu slice (read with weight 0 where nu = 1
-  // selects the last slice) and one entry (read with weight 0 where the mu_s
-  // position is the slice's last texel)
+  const int slab_stride = sh.R * 3 * SR;
+  // zero guard after each plane row: a nu slice (read with weight 0 where
+  // nu = 1 selects the last slice) and one entry (read with weight 0 where the
+  // mu_s position is the slice's last texel)
   const int ng = NM + 1;
-  for (int k = tid; k < kMsSlabs * nrow * ng; k += nth) {
-    const int b = k / (nrow * ng), rem = k % (nrow * ng);
-    slab[b * slab_stride + (rem / ng) * SR + W + rem % ng] = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (int k = tid; k < kMsSlabs * nrow * 3 * ng; k += nth) {
+    const int pl = k / ng;  // plane row: slab pl / (3 nrow), row and plane pl % (3 nrow)
+    slab[(pl / (3 * nrow)) * slab_stride + (pl % (3 * nrow)) * SR + W + k % ng] = 0.f;
   }
   {  // this tile's sample records, their density row offsets bounded to the table
     static_assert(sizeof(MSRec) == 4 * sizeof(int4) && offsetof(MSRec, off) == 3 * sizeof(int4),
                   "MSRec: four 16-byte words, the offsets last");
     const int4* src = reinterpret_cast<const int4*>(a.g_ms + (size_t)row0 * NS);
     int4* dst = reinterpret_cast<int4*>(rec);
-    const int omax = (a.sc_r * a.sc_mu - 1) * W;  // start of the table's last row
+    const int omax = (a.sc_r * a.sc_mu - 1) * (3 * a.Wd / 4);  // start of the table's last row
     for (int k = tid; k < nrow * NS; k += nth) {
       int4 o = __ldg(src + 4 * k + 3);
       o.x = min(max(o.x, 0), omax);
@@ -1498,6 +1503,21 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
   // per-texel constants (TPT texels per thread): row, slab entry, texel x
   float c_rmus[TPT], c_nu[TPT], c_lerp[TPT];
   int c_lr[TPT], c_e[TPT], c_x[TPT];
+  // per-unit constants of the slab build (TPT units per thread; a unit is
+  // four entries of one plane of a row, and a tile has at most as many units
+  // as texels since rows are at least 4 entries wide): row, float offset in
+  // the density row, slab offset, entries in use
+  const int G4 = (W + 3) / 4, nunits = nrow * 3 * G4;
+  int u_lr[TPT], u_src[TPT], u_dst[TPT], u_n[TPT];
+#pragma unroll
+  for (int j = 0; j < TPT; ++j) {
+    const int u = tid + j * nth;
+    const int lr = u / (3 * G4), rem = u - lr * 3 * G4, pl = rem / G4, g = rem - pl * G4;
+    u_lr[j] = lr;
+    u_src[j] = pl * a.Wd + 4 * g;
+    u_dst[j] = (lr * 3 + pl) * SR + 4 * g;
+    u_n[j] = min(4, W - 4 * g);
+  }
   Kahan3 acc[TPT];
   float3 part[TPT];
   MuS32 mus32;
@@ -1512,7 +1532,7 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
     const int k = tid + j * nth;
     c_lr[j] = k / W;
     c_x[j] = k - c_lr[j] * W;
-    c_e[j] = c_lr[j] * SR;
+    c_e[j] = c_lr[j] * 3 * SR;
     if (k < nx_tex) {
       float mu_s, nu, rmus;
       texel_mus_nu<MX>(a.g_rows[row0 + c_lr[j]], a.g_cols[c_x[j]], mu_s, nu, rmus);
@@ -1526,44 +1546,53 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
     }
   }
   __syncthreads();
-  const float4* dens = a.dens;
+  const float* dens = a.dens;
   // Slab of sample i: the density table interpolated in (mu, r) at the
   // sample, for the tile's slices of the row. With one texel per thread its
   // four loads are issued one sample ahead (load) and blended after the texel
   // work (blend); with more, the registers are not there and the loads
-  // directly precede the blend.
+  // directly precede the blend. The last unit of a plane row reads up to
+  // three entries of the density table's padding and stores only those in
+  // use, leaving the zero guard alone.
   constexpr bool kAhead = TPT == 1;
   float4 q[TPT][4];
   auto load = [&](int i) {
 #pragma unroll
     for (int j = 0; j < TPT; ++j) {
-      if (tid + j * nth < nx_tex) {
-        const MSRec& o = rec[c_lr[j] * NS + i];
-        const float4* p = dens + c_x[j];
+      if (tid + j * nth < nunits) {
+        const MSRec& o = rec[u_lr[j] * NS + i];
+        const float4* p = reinterpret_cast<const float4*>(dens + u_src[j]);
 #pragma unroll
         for (int c = 0; c < 4; ++c) q[j][c] = ld4(p + o.off[c]);
       }
     }
   };
-  auto blend = [&](int i, float4* dst) {
+  auto blend = [&](int i, float* dst) {
 #pragma unroll
     for (int j = 0; j < TPT; ++j) {
-      if (tid + j * nth < nx_tex) {
-        const MSRec& o = rec[c_lr[j] * NS + i];
+      if (tid + j * nth < nunits) {
+        const MSRec& o = rec[u_lr[j] * NS + i];
         const float w00 = o.w[0], w10 = o.w[1], w01 = o.w[2], w11 = o.w[3];
         const float4 a00 = q[j][0], a10 = q[j][1], a01 = q[j][2], a11 = q[j][3];
         float4 v;
         v.x = fmaf(w11, a11.x, fmaf(w01, a01.x, fmaf(w10, a10.x, w00 * a00.x)));
         v.y = fmaf(w11, a11.y, fmaf(w01, a01.y, fmaf(w10, a10.y, w00 * a00.y)));
         v.z = fmaf(w11, a11.z, fmaf(w01, a01.z, fmaf(w10, a10.z, w00 * a00.z)));
-        v.w = 0.f;
-        dst[c_lr[j] * SR + c_x[j]] = v;
+        v.w = fmaf(w11, a11.w, fmaf(w01, a01.w, fmaf(w10, a10.w, w00 * a00.w)));
+        float* d = dst + u_dst[j];
+        if (u_n[j] == 4) {
+          *reinterpret_cast<float4*>(d) = v;
+        } else {
+          d[0] = v.x;
+          if (u_n[j] > 1) d[1] = v.y;
+          if (u_n[j] > 2) d[2] = v.z;
+        }
       }
     }
   };
   const float fmus = float(NM);
   // the texel work of sample i on its slab
-  auto step = [&](int i, const float4* cur) {
+  auto step = [&](int i, const float* cur) {
 #pragma unroll
     for (int j = 0; j < TPT; ++j) {
       if (tid + j * nth < nx_tex) {
@@ -1581,12 +1610,13 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
         }
         float fx;
         const int i0 = row_pos(t, fmus - 1.0f, fx);
-        const float4* sl = cur + c_e[j] + i0;
-        const float4 p00 = sl[0], p01 = sl[1], p10 = sl[NM], p11 = sl[NM + 1];
+        const float* sl = cur + c_e[j] + i0;
+        const float* sg = sl + SR;
+        const float* sb = sl + 2 * SR;
         const float lf = c_lerp[j];
-        const float ax = fmaf(p01.x - p00.x, fx, p00.x), bx = fmaf(p11.x - p10.x, fx, p10.x);
-        const float ay = fmaf(p01.y - p00.y, fx, p00.y), by = fmaf(p11.y - p10.y, fx, p10.y);
-        const float az = fmaf(p01.z - p00.z, fx, p00.z), bz = fmaf(p11.z - p10.z, fx, p10.z);
+        const float ax = fmaf(sl[1] - sl[0], fx, sl[0]), bx = fmaf(sl[NM + 1] - sl[NM], fx, sl[NM]);
+        const float ay = fmaf(sg[1] - sg[0], fx, sg[0]), by = fmaf(sg[NM + 1] - sg[NM], fx, sg[NM]);
+        const float az = fmaf(sb[1] - sb[0], fx, sb[0]), bz = fmaf(sb[NM + 1] - sb[NM], fx, sb[NM]);
         const float3 J = make_float3(fmaf(bx - ax, lf, ax), fmaf(by - ay, lf, ay), fmaf(bz - az, lf, az));
         const float3 v = J * make_float3(o.tvwx, o.tvwy, o.tvwz);
         if (!MX) {

@@ -217,7 +217,11 @@ typedef struct fb_intermediates {
     void* delta_rayleigh;
     void* delta_mie;
     void* delta_multiple_scattering;
+    /* float planes: for each (r, mu) row of the scattering extent, R then G
+     * then B, each scattering_density_stride floats of which the first
+     * width (nu_size * mu_s_size) hold values */
     void* scattering_density;
+    uint32_t scattering_density_stride;
 } fb_intermediates;
 int fb_pending_intermediates(fb_pending* p, uint32_t index, fb_intermediates* out);
 /* Drop for PendingAtmosphere (src/precompute.rs:2122-2140): frees the

@@ -126,6 +126,7 @@ pub struct fb_intermediates {
     pub delta_mie: *mut c_void,
     pub delta_multiple_scattering: *mut c_void,
     pub scattering_density: *mut c_void,
+    pub scattering_density_stride: u32,
 }
 
 #[repr(C)]
