@@ -767,11 +767,16 @@ __host__ __device__ inline DensShape dens_shape(int sc_r, int sc_mu, int sc_mus,
   return d;
 }
 
-// One interval [k, k + 1] of a linearly interpolated RGB table: the value at
-// its midpoint k + 1/2 in a.xyz, the difference of its two entries in
-// (a.w, b.x, b.y); 32 bytes, read as one 16- and one 8-byte load from the same
-// base address. The value at position t in the interval is
-// a.xyz + (t - k - 1/2) (a.w, b.x, b.y).
+// One interval [k, k + 1] of a linearly interpolated RGB table, as the line
+// through its two entries in the variable w = t - 1/2 (t the texel position):
+// the line's value at w = 0 in a.xyz and its slope, the difference of the two
+// entries, in (a.w, b.x, b.y); 32 bytes, read as one 16- and one 8-byte load
+// from the same base address. The value at w in the interval is
+// a.xyz + w (a.w, b.x, b.y): one FMA per channel, no offset within the
+// interval to form. The line's value at 0 is left entry + (1/2 - k) slope,
+// which rounds with the magnitude of k times the slope; k is at most the
+// table size, so the error stays a few units in the last place of the
+// table's largest values.
 struct LerpRec {
   float4 a;
   float2 b;
@@ -868,17 +873,15 @@ struct PhaseCoef {
 // w = t - 1/2 directly, with the scale folded into their direction tables.
 // Rounding w to an integer k through the float adder (adding 1.5 * 2^23) gives
 // the interval [k, k + 1] that holds t (or, where t is an integer, the
-// neighbouring one: the same value), fr = w - k in [-1/2, 1/2] its offset from
-// the interval's midpoint, and the record position in a table of n records:
-// k & (n - 1) (the float's low bits; 1.5 * 2^23 has none set), or for CL
-// k + 1 clamped to [0, n - 1] (negative values wrap to large unsigned ones).
+// neighbouring one: the same value) and its record position in a table of n
+// records: k & (n - 1) (the float's low bits; 1.5 * 2^23 has none set), or for
+// CL k + 1 clamped to [0, n - 1] (negative values wrap to large unsigned ones).
 // Rounding excursions of c just beyond [-1, 1] give k = -1 or k = n - 1,
 // whose records extrapolate by the excursion.
 constexpr float kRoundMagic = 12582912.0f;  // 1.5 * 2^23
 constexpr int kRoundMagicBits = 0x4B400000;
-template <bool CL> __device__ __forceinline__ int mid_pos(float w, int n, float& fr) {
+template <bool CL> __device__ __forceinline__ int line_pos(float w, int n) {
   const float y = w + kRoundMagic;
-  fr = w - (y - kRoundMagic);
   if (CL) return (int)min((unsigned)(__float_as_int(y) - (kRoundMagicBits - 1)), (unsigned)(n - 1));
   return __float_as_int(y) & (n - 1);
 }
@@ -888,7 +891,7 @@ template <bool CL> __device__ __forceinline__ int mid_pos(float w, int n, float&
 // (scattering.h:139-179), plus for rows that meet the ground the ground
 // bounce (scattering_density.comp:64-84), times the phase functions
 // (scattering_density.comp:86-104). Table positions come as w = t - 1/2
-// (mid_pos): the direction table holds cos phi sin t and sin phi sin t scaled
+// (line_pos): the direction table holds cos phi sin t and sin phi sin t scaled
 // by (nu_size - 1) / 2 and the ground normal scaled by (ir_mus - 1) / 2, and
 // the row and column terms carry the offsets.
 struct DensRowConst {
@@ -920,11 +923,10 @@ __device__ __forceinline__ void dens_row(const DensLayout& S, const DensTheta& t
 #pragma unroll
         for (int side = 0; side < 2; ++side) {
           const float w = side ? base - dy : base + dy;
-          float fr;
-          const int k = mid_pos<CL>(w, q.nP, fr);
+          const int k = line_pos<CL>(w, q.nP);
           const float4 pa = Pl[k].a;
           const float2 pb = Pl[k].b;
-          float3 inc = make_float3(fmaf(pa.w, fr, pa.x), fmaf(pb.x, fr, pa.y), fmaf(pb.y, fr, pa.z));
+          float3 inc = make_float3(fmaf(pa.w, w, pa.x), fmaf(pb.x, w, pa.y), fmaf(pb.y, w, pa.z));
           if (TWO) {
             // R P_R(nu) + M P_M(nu) = (1 + nu^2) (kR R + kM (1 + g^2 - 2 g nu)^-3/2 M),
             // the constants kR, kM folded into the tables
@@ -934,20 +936,19 @@ __device__ __forceinline__ void dens_row(const DensLayout& S, const DensTheta& t
             const float t1 = fmaf(nu1, nu1, 1.0f);
             const float rs = rsqrtf(fmaf(-pc.g2, nu1, pc.g1));
             const float rs3 = rs * rs * rs;
-            inc.x = fmaf(fmaf(qa.w, fr, qa.x), rs3, inc.x) * t1;
-            inc.y = fmaf(fmaf(qb.x, fr, qa.y), rs3, inc.y) * t1;
-            inc.z = fmaf(fmaf(qb.y, fr, qa.z), rs3, inc.z) * t1;
+            inc.x = fmaf(fmaf(qa.w, w, qa.x), rs3, inc.x) * t1;
+            inc.y = fmaf(fmaf(qb.x, w, qa.y), rs3, inc.y) * t1;
+            inc.z = fmaf(fmaf(qb.y, w, qa.z), rs3, inc.z) * t1;
           }
           if (GROUND) {
             // irradiance of order n - 2 where omega_i meets the ground
             const float we = side ? gb - gdy : gb + gdy;
-            float fe;
-            const int e = mid_pos<CL>(we, q.nE, fe);
+            const int e = line_pos<CL>(we, q.nE);
             const float4 ea = S.E[e].a;
             const float2 eb = S.E[e].b;
-            inc.x = fmaf(t.tgx, fmaf(ea.w, fe, ea.x), inc.x);
-            inc.y = fmaf(t.tgy, fmaf(eb.x, fe, ea.y), inc.y);
-            inc.z = fmaf(t.tgz, fmaf(eb.y, fe, ea.z), inc.z);
+            inc.x = fmaf(t.tgx, fmaf(ea.w, we, ea.x), inc.x);
+            inc.y = fmaf(t.tgy, fmaf(eb.x, we, ea.y), inc.y);
+            inc.z = fmaf(t.tgz, fmaf(eb.y, we, ea.z), inc.z);
           }
           acc[j].x = fmaf(inc.x, cf.x, acc[j].x);
           acc[j].y = fmaf(inc.y, cf.y, acc[j].y);
@@ -1018,9 +1019,9 @@ __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned cha
   // --- reduced tables: the previous order's table at this tile's r and mu_s
   // columns, on the theta rows, as nu intervals: the entries (pass 1), the
   // differences (pass 2, into b and pad, which pass 1 readers do not touch),
-  // then midpoint and difference in place (pass 3); the same for the ground
-  // irradiance row; direction pairs with ground normals, pre-scaled for
-  // mid_pos
+  // then the line's value at w = 0 and its slope in place (pass 3); the same
+  // for the ground irradiance row; direction pairs with ground normals,
+  // pre-scaled for line_pos
   const int MK = dens_mk(NNU, CL), MKE = dens_mke(a.ir_mus, CL);
   const size_t nPtab = (size_t)sh.S * NT * MK;
   const int per_col = NT * MK;
@@ -1103,14 +1104,18 @@ __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned cha
     }
   }
   __syncthreads();
-  {  // pass 3: midpoint value and difference, in the record's own fields
-    auto mid = [](LerpRec& rec) {
+  {  // pass 3: the line of interval ki, value at w = 0 and slope, in the record's own fields
+    auto line = [](LerpRec& rec, int ki) {
       const float3 d = make_float3(rec.b.x, rec.b.y, rec.pad.x);
-      rec.a = make_float4(fmaf(0.5f, d.x, rec.a.x), fmaf(0.5f, d.y, rec.a.y), fmaf(0.5f, d.z, rec.a.z), d.x);
+      const float c = 0.5f - float(ki);
+      rec.a = make_float4(fmaf(c, d.x, rec.a.x), fmaf(c, d.y, rec.a.y), fmaf(c, d.z, rec.a.z), d.x);
       rec.b = make_float2(d.y, d.z);
     };
-    for (int k = tid; k < ntab * ns * per_col; k += nth) mid(S.P[(k / (ns * per_col)) * nPtab + k % (ns * per_col)]);
-    for (int k = tid; k < MKE; k += nth) mid(S.E[k]);
+    for (int k = tid; k < ntab * ns * per_col; k += nth) {
+      const int kk = k % (ns * per_col);
+      line(S.P[(k / (ns * per_col)) * nPtab + kk], rec_interval<CL>(kk % MK, MK));
+    }
+    for (int k = tid; k < MKE; k += nth) line(S.E[k], rec_interval<CL>(k, MKE));
   }
   __syncthreads();
 
