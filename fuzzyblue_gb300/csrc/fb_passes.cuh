@@ -1637,45 +1637,60 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
       }
     }
   };
-  auto slab_of = [&](int i) { return slab + (i % kMsSlabs) * slab_stride; };
+  // sample i lives in slab buffer i % kMsSlabs; with one texel per thread the
+  // mixed loop runs four samples per iteration so that every buffer is a
+  // fixed pointer (with two, the longer body spills)
+  float* const sb0 = slab;
+  float* const sb1 = slab + slab_stride;
+  float* const sb2 = slab + 2 * slab_stride;
+  float* const sb3 = slab + 3 * slab_stride;
+  static_assert(kMsSlabs == 4, "four slab buffers");
+  // sample k from `cur` while sample k + A is built into `nxt`
+  auto visit = [&](int k, const float* cur, float* nxt, int A) {
+    if (k < NS) {
+      if (kAhead && k + A < NS) load(k + A);
+      step(k, cur);
+      if (k + A < NS) {
+        if (!kAhead) load(k + A);
+        blend(k + A, nxt);
+      }
+    }
+  };
   if (MX) {
     // two samples per barrier: i and i + 1 from their slabs while i + 2 and
     // i + 3 are built (measured faster for the mixed kernels; the plain ones
     // run faster one sample per barrier)
     load(0);
-    blend(0, slab_of(0));
+    blend(0, sb0);
     if (NS > 1) {
       load(1);
-      blend(1, slab_of(1));
+      blend(1, sb1);
     }
     __syncthreads();
-    for (int i = 0; i < NS; i += 2) {
-#pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int k = i + h;
-        if (k < NS) {
-          if (kAhead && k + 2 < NS) load(k + 2);
-          step(k, slab_of(k));
-          if (k + 2 < NS) {
-            if (!kAhead) load(k + 2);
-            blend(k + 2, slab_of(k + 2));
-          }
-        }
+    if (TPT == 1) {
+      for (int i = 0; i < NS; i += 4) {
+        visit(i, sb0, sb2, 2);
+        visit(i + 1, sb1, sb3, 2);
+        __syncthreads();
+        visit(i + 2, sb2, sb0, 2);
+        visit(i + 3, sb3, sb1, 2);
+        __syncthreads();
       }
-      __syncthreads();
+    } else {
+      for (int i = 0; i < NS; i += 2) {
+        visit(i, slab + (i % kMsSlabs) * slab_stride, slab + ((i + 2) % kMsSlabs) * slab_stride, 2);
+        visit(i + 1, slab + ((i + 1) % kMsSlabs) * slab_stride, slab + ((i + 3) % kMsSlabs) * slab_stride, 2);
+        __syncthreads();
+      }
     }
   } else {
-    // one sample per barrier: i from its slab while i + 1 is built
+    // one sample per barrier: i from its slab while i + 1 is built (a
+    // four-sample body with fixed buffers measured slower here)
     load(0);
-    blend(0, slab_of(0));
+    blend(0, sb0);
     __syncthreads();
     for (int i = 0; i < NS; ++i) {
-      if (kAhead && i + 1 < NS) load(i + 1);
-      step(i, slab_of(i));
-      if (i + 1 < NS) {
-        if (!kAhead) load(i + 1);
-        blend(i + 1, slab_of(i + 1));
-      }
+      visit(i, slab + (i % kMsSlabs) * slab_stride, slab + ((i + 1) % kMsSlabs) * slab_stride, 1);
       __syncthreads();
     }
   }
