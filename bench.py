@@ -423,7 +423,7 @@ def run_ours(a):
         td.destroy_process_group()
 
 
-def cpu_baseline(p, fraction=1.0 / 8):
+def cpu_baseline(p, fraction=1.0):
     from oracle import cpu_baseline as C
     kind = "reference" if C.reference_available() else "port"
     r = C.estimate(p, "reference" if kind == "reference" else "port", fraction=fraction)

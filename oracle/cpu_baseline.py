@@ -125,5 +125,6 @@ def estimate(p: Parameters, impl: str = "port", fraction: float = 1.0 / 32, seed
         "passes": {k: {"sample_texels": int(n), "texels": int(t), "runs": int(r), "seconds": round(dt, 4)}
                    for k, (dt, n, t, r) in timings.items()},
         "sample": "every pass of one atmosphere on a fixed random %.4g of its texels (density %.4g, indirect %.4g), "
-                  "scaled by texel count and order count" % (fraction, fraction / 4, fraction * 4),
+                  "scaled by texel count and order count; %.1f s on the host" % (
+                      min(fraction, 1.0), min(fraction / 4, 1.0), min(fraction * 4, 1.0), measured),
     }
