@@ -543,13 +543,15 @@ __host__ __device__ inline int tiles_densgeo(int sc_r, int dens_n) {
 
 // ============================================================ S: single ===
 // Per (row, sample) of single scattering; 16-byte words in the order the
-// texel loop reads them, so that each is one shared load.
+// texel loop reads them, so that each is one shared load. tr and tm are the
+// transmittance from the texel times the trapezoid weight times the Rayleigh
+// and Mie densities at the sample.
 struct __align__(16) SSRec {
   float d, inv_r, r_d, rr_d;
   float e, dmin, inv_span, cos_h;
-  float lo, inv_w, fy, w;
-  float tvx, tvy, tvz, rho_r;
-  float rho_m;
+  float lo, inv_w, fy, trx;
+  float try_, trz, tmx, tmy;
+  float tmz;
   int y0, y1, pad;
 };
 
@@ -573,8 +575,9 @@ __device__ void tile_single(const DevAtmo& a, int tile, unsigned char* smem) {
     const int i = k % NS;
     SSRec& o = rec[k];
     o.pad = 0;
-    o.w = (i == 0 || i == N) ? 0.5f : 1.0f;
+    const float w = (i == 0 || i == N) ? 0.5f : 1.0f;
     float3 tv;
+    float rho_r, rho_m;
     if (!MX) {
       Geo32 G;
       G.init(a);
@@ -588,8 +591,8 @@ __device__ void tile_single(const DevAtmo& a, int tile, unsigned char* smem) {
       o.r_d = r_d;
       o.rr_d = r_d * r_d;
       float h = r_d - G.R;
-      o.rho_r = profile_density(a.ray_d, h);
-      o.rho_m = profile_density(a.mie_d, h);
+      rho_r = profile_density(a.ray_d, h);
+      rho_m = profile_density(a.mie_d, h);
       // transmittance.h:63-74 and :7-24
       float sin_h = G.R / r_d;
       o.cos_h = -sqrtf(gmax(1.0f - sin_h * sin_h, 0.0f));
@@ -618,8 +621,8 @@ __device__ void tile_single(const DevAtmo& a, int tile, unsigned char* smem) {
       o.r_d = r_d;
       o.rr_d = 0.f;
       const float h = __fdividef(qf, r_d + G.R);
-      o.rho_r = profile_density(a.ray_d, h);
-      o.rho_m = profile_density(a.mie_d, h);
+      rho_r = profile_density(a.ray_d, h);
+      rho_m = profile_density(a.mie_d, h);
       const float rho = sqrtf(qf);
       o.inv_r = 1.0f / r_d;
       o.cos_h = -rho * o.inv_r;
@@ -635,9 +638,13 @@ __device__ void tile_single(const DevAtmo& a, int tile, unsigned char* smem) {
       o.y1 = ay.i1;
       o.fy = ay.f;
     }
-    o.tvx = tv.x;
-    o.tvy = tv.y;
-    o.tvz = tv.z;
+    const float wr = w * rho_r, wm = w * rho_m;
+    o.trx = tv.x * wr;
+    o.try_ = tv.y * wr;
+    o.trz = tv.z * wr;
+    o.tmx = tv.x * wm;
+    o.tmy = tv.y * wm;
+    o.tmz = tv.z * wm;
   }
   __syncthreads();
   const float TT = a.top * a.top;
@@ -679,14 +686,13 @@ __device__ void tile_single(const DevAtmo& a, int tile, unsigned char* smem) {
       ay.i1 = o.y1;
       ay.f = o.fy;
       const float3 ts = fetch2(a.tr, a.tr_mu, ax, ay) * sfac;
-      const float3 t3 = make_float3(o.tvx, o.tvy, o.tvz) * ts;
-      const float3 ri_ = t3 * o.rho_r, mi_ = t3 * o.rho_m;
+      const float3 ri_ = ts * make_float3(o.trx, o.try_, o.trz), mi_ = ts * make_float3(o.tmx, o.tmy, o.tmz);
       if (!MX) {
-        ray.s = ray.s + ri_ * o.w;
-        mie.s = mie.s + mi_ * o.w;
+        ray.s = ray.s + ri_;
+        mie.s = mie.s + mi_;
       } else {
-        ray.add(ri_ * o.w);
-        mie.add(mi_ * o.w);
+        ray.add(ri_);
+        mie.add(mi_);
       }
     }
     const float dx = MX ? (float)(ri.distd / double(N)) : ri.dist / float(N);
