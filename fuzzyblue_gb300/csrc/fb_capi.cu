@@ -195,7 +195,7 @@ TableSizes sizes_of(const fb_params& p) {
   s.out_bytes = align256(16 * s.ntr) + align256(16 * s.nir) + align256(16 * s.nsc);
   const size_t rows = (size_t)r.scattering_mu_size * r.scattering_r_size;
   s.dens_bytes = 12 * rows * (size_t)fb::dens_stride((int)(r.scattering_nu_size * r.scattering_mu_s_size));
-  s.tmp_bytes = 2 * align256(16 * s.nir) + 3 * align256(16 * s.nsc) + align256(s.dens_bytes);
+  s.tmp_bytes = align256(32 * s.ntr) + 2 * align256(16 * s.nir) + 3 * align256(16 * s.nsc) + align256(s.dens_bytes);
   if (p.precision == FB_PRECISION_MIXED) s.tmp_bytes += align256(24 * s.nsc) + align256(24 * s.nir);
   s.tmp_bytes += geometry_bytes(p);
   return s;
@@ -754,6 +754,7 @@ int build(fb_builder* b, cudaStream_t s, const fb_params* params, uint32_t count
     d.ir = a->ir;
     d.sc = a->sc;
     const TableSizes& z = sz[i];
+    d.trp = (float*)tp;      tp += align256(32 * z.ntr);
     d.dirr[0] = (float4*)tp; tp += align256(16 * z.nir);
     d.dirr[1] = (float4*)tp; tp += align256(16 * z.nir);
     d.dr = (float4*)tp;      tp += align256(16 * z.nsc);

@@ -113,6 +113,8 @@ struct DevAtmo {
   float4* ir;
   float4* sc;
   // temporaries
+  float* trp;       // transmittance pairs: per texel (mu i, r j) 32 bytes, the RGB of
+                    // texels i and min(i + 1, tr_mu - 1) of row j and two zeros
   float4* dirr[2];  // delta irradiance, ping-pong by order parity
   float4* dr;       // delta Rayleigh (single)
   float4* dm;       // delta Mie (single)
@@ -219,6 +221,27 @@ __device__ __forceinline__ float3 fetch2(const float4* t, int w, Axis x, Axis y)
   o.x = fmaf(w11, p11.x, fmaf(w01, p01.x, fmaf(w10, p10.x, w00 * p00.x)));
   o.y = fmaf(w11, p11.y, fmaf(w01, p01.y, fmaf(w10, p10.y, w00 * p00.y)));
   o.z = fmaf(w11, p11.z, fmaf(w01, p01.z, fmaf(w10, p10.z, w00 * p00.z)));
+  return o;
+}
+
+// The same bilinear fetch from the transmittance pair table: one 32-byte load
+// per row brings both x neighbours. Needs x.i1 = min(x.i0 + 1, w - 1), which
+// axis_texel gives for coordinates t >= 0.
+__device__ __forceinline__ void ld_pair(const float* p, float4& lo, float4& hi) {
+  asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=f"(lo.x), "=f"(lo.y), "=f"(lo.z), "=f"(lo.w), "=f"(hi.x), "=f"(hi.y), "=f"(hi.z), "=f"(hi.w)
+      : "l"(p));
+}
+__device__ __forceinline__ float3 fetch2_pairs(const float* trp, int w, Axis x, Axis y) {
+  float4 a0, a1, b0, b1;  // row y0: (p00.xyz, p10.x) (p10.yz, 0, 0); row y1 likewise
+  ld_pair(trp + 8 * (size_t)(y.i0 * w + x.i0), a0, a1);
+  ld_pair(trp + 8 * (size_t)(y.i1 * w + x.i0), b0, b1);
+  const float w00 = (1.0f - x.f) * (1.0f - y.f), w10 = x.f * (1.0f - y.f);
+  const float w01 = (1.0f - x.f) * y.f, w11 = x.f * y.f;
+  float3 o;
+  o.x = fmaf(w11, b0.w, fmaf(w01, b0.x, fmaf(w10, a0.w, w00 * a0.x)));
+  o.y = fmaf(w11, b1.x, fmaf(w01, b0.y, fmaf(w10, a1.x, w00 * a0.y)));
+  o.z = fmaf(w11, b1.y, fmaf(w01, b0.z, fmaf(w10, a1.y, w00 * a0.z)));
   return o;
 }
 

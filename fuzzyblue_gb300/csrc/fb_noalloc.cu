@@ -145,6 +145,7 @@ extern "C" int fb_atmosphere_build_noalloc(void* stream, const fb_params* p, voi
   d.ir = (float4*)irradiance;
   d.sc = (float4*)scattering;
   unsigned char* tp = base + o_tmp;
+  d.trp = (float*)tp;      tp += align256(32 * z.ntr);
   d.dirr[0] = (float4*)tp; tp += align256(16 * z.nir);
   d.dirr[1] = (float4*)tp; tp += align256(16 * z.nir);
   d.dr = (float4*)tp;      tp += align256(16 * z.nsc);

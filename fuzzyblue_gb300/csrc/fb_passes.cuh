@@ -187,6 +187,24 @@ template <bool MX> __device__ void tile_transmittance(const DevAtmo& a, int tile
     o.z = expf(-(a.rayleigh[2] * sR + a.mie_ext[2] * sM + a.absorption[2] * sA));
     o.w = 1.0f;
     a.tr[t] = o;
+    // the pair table: this texel's RGB first in its own record, second in the
+    // record of texel i - 1 and, at the last mu, in its own
+    const int i = t % a.tr_mu;
+    float* own = a.trp + 8 * (size_t)t;
+    own[0] = o.x;
+    own[1] = o.y;
+    own[2] = o.z;
+    own[6] = own[7] = 0.f;
+    if (i > 0) {
+      own[-5] = o.x;
+      own[-4] = o.y;
+      own[-3] = o.z;
+    }
+    if (i == a.tr_mu - 1) {
+      own[3] = o.x;
+      own[4] = o.y;
+      own[5] = o.z;
+    }
   }
 }
 
@@ -679,13 +697,15 @@ __device__ void tile_single(const DevAtmo& a, int tile, unsigned char* smem) {
       // smoothstep(-sin_h alpha, sin_h alpha, mu_s_d - cos_h)
       const float st = gclamp((mu_s_d - o.cos_h - o.lo) * o.inv_w, 0.0f, 1.0f);
       const float sfac = st * st * (3.0f - 2.0f * st);
-      const Axis ax = MX ? axis_texel(x_mu * float(a.tr_mu - 1), a.tr_mu)
-                         : axis_texel(fmaf(fmaf(x_mu, trc1, trc0), trn, -0.5f), a.tr_mu);
+      // below the first texel centre (only by rounding) the sampler's clamp
+      // gives texel 0 alone, as t = 0 does: the pair fetch needs t >= 0
+      const Axis ax = MX ? axis_texel(fmaxf(x_mu * float(a.tr_mu - 1), 0.0f), a.tr_mu)
+                         : axis_texel(fmaxf(fmaf(fmaf(x_mu, trc1, trc0), trn, -0.5f), 0.0f), a.tr_mu);
       Axis ay;
       ay.i0 = o.y0;
       ay.i1 = o.y1;
       ay.f = o.fy;
-      const float3 ts = fetch2(a.tr, a.tr_mu, ax, ay) * sfac;
+      const float3 ts = fetch2_pairs(a.trp, a.tr_mu, ax, ay) * sfac;
       const float3 ri_ = ts * make_float3(o.trx, o.try_, o.trz), mi_ = ts * make_float3(o.tmx, o.tmy, o.tmz);
       if (!MX) {
         ray.s = ray.s + ri_;
