@@ -732,7 +732,9 @@ __device__ void tile_single(const DevAtmo& a, int tile, unsigned char* smem) {
   }
 }
 
-template <bool MX> __global__ void __launch_bounds__(kThreads) k_single(LaunchArgs L) {
+// Registers capped for 4 resident CTAs per SM (a few bytes of spills in the
+// mixed kernel).
+template <bool MX> __global__ void __launch_bounds__(kThreads, 4) k_single(LaunchArgs L) {
   extern __shared__ __align__(16) unsigned char smem[];
   int seg, job, tile;
   int taken = 0;
