@@ -810,6 +810,14 @@ struct LerpRec {
   float2 b;
   float2 pad;
 };
+// Order 2: the Rayleigh and Mie intervals of the same nu position in one
+// 48-byte record, read as three 16-byte loads: a = (R value at 0, R slope x),
+// b = (R slope y, R slope z, M value at 0 x, y), c = (M value at 0 z, M slope).
+// Records 48 bytes apart also put the intervals 0-7 of a row on disjoint
+// banks for each 16-byte load.
+struct LerpRec2 {
+  float4 a, b, c;
+};
 
 // The density tile's interval tables have a power-of-two number of records,
 // addressed by k & (size - 1): intervals k >= 0 at position k, the interval
@@ -839,7 +847,8 @@ struct DensLayout {
   float4* dir;      // NT * NT mirror pairs: (cos phi sin t, sin phi sin t) x (nu_size - 1) / 2,
                     // (ground normal x, y) x (ir_mus - 1) / 2
   float* gnz;       // NT * NT: ground normal z x (ir_mus - 1) / 2
-  LerpRec* P;       // per table, S * NT * MK: nu intervals of the previous order (dens_mk)
+  LerpRec* P;       // S * NT * MK: nu intervals of the previous order (dens_mk); order 2:
+                    // LerpRec2 records of the Rayleigh and Mie tables
   LerpRec* E;       // MKE: intervals of the ground irradiance row, the two sampler rows pre-blended (dens_mke)
   float* col_mus;   // S
   double* col_musd; // S (MIXED)
@@ -851,7 +860,7 @@ struct DensLayout {
 __host__ __device__ inline size_t dens_layout(unsigned char* base, int dens_n, int sc_nu, int ir_mus, int S,
                                               int chunk, bool two, bool mixed, bool cl, DensLayout* L) {
   const int NT = dens_n, NK = sc_nu + 2;
-  const size_t nP = (size_t)S * NT * dens_mk(sc_nu, cl) * (two ? 2 : 1);
+  const size_t nP = (size_t)S * NT * dens_mk(sc_nu, cl);
   size_t o = 0;
   auto take = [&](size_t bytes) {
     size_t at = o;
@@ -860,7 +869,7 @@ __host__ __device__ inline size_t dens_layout(unsigned char* base, int dens_n, i
   };
   size_t o_th = take(sizeof(DensTheta) * NT), o_tay = take(sizeof(Axis) * NT), o_kax = take(sizeof(Axis) * S * NK);
   size_t o_dir = take(sizeof(float4) * NT * NT), o_gnz = take(sizeof(float) * NT * NT);
-  size_t o_P = take(sizeof(LerpRec) * nP), o_E = take(sizeof(LerpRec) * dens_mke(ir_mus, cl));
+  size_t o_P = take((two ? sizeof(LerpRec2) : sizeof(LerpRec)) * nP), o_E = take(sizeof(LerpRec) * dens_mke(ir_mus, cl));
   size_t o_cm = take(sizeof(float) * S), o_cmd = take(sizeof(double) * S);
   size_t o_ymu = take(mixed ? sizeof(double2) * chunk : 0), o_nu = take(mixed ? sizeof(double) * sc_nu : 0);
   size_t o_acc = take(mixed ? sizeof(float) * kDensThreads * kDensMaxGroup * 6 : 0);
@@ -930,7 +939,7 @@ struct DensRowConst {
 };
 template <bool TWO, bool GROUND, bool CL>
 __device__ __forceinline__ void dens_row(const DensLayout& S, const DensTheta& t, int l, int NT,
-                                         const LerpRec* __restrict__ Pl, const LerpRec* __restrict__ Ml,
+                                         const LerpRec* __restrict__ Pl,
                                          const DensRowConst& q, const float (&sx)[kDensMaxGroup],
                                          const float (&sy)[kDensMaxGroup], int G, const PhaseCoef& pc,
                                          float3 (&acc)[kDensMaxGroup]) {
@@ -952,21 +961,23 @@ __device__ __forceinline__ void dens_row(const DensLayout& S, const DensTheta& t
         for (int side = 0; side < 2; ++side) {
           const float w = side ? base - dy : base + dy;
           const int k = line_pos<CL>(w, q.nP);
-          const float4 pa = Pl[k].a;
-          const float2 pb = Pl[k].b;
-          float3 inc = make_float3(fmaf(pa.w, w, pa.x), fmaf(pb.x, w, pa.y), fmaf(pb.y, w, pa.z));
-          if (TWO) {
+          float3 inc;
+          if (!TWO) {
+            const float4 pa = Pl[k].a;
+            const float2 pb = Pl[k].b;
+            inc = make_float3(fmaf(pa.w, w, pa.x), fmaf(pb.x, w, pa.y), fmaf(pb.y, w, pa.z));
+          } else {
             // R P_R(nu) + M P_M(nu) = (1 + nu^2) (kR R + kM (1 + g^2 - 2 g nu)^-3/2 M),
             // the constants kR, kM folded into the tables
+            const LerpRec2& r2 = reinterpret_cast<const LerpRec2*>(Pl)[k];
+            const float4 ra = r2.a, rb = r2.b, rc = r2.c;
             const float nu1 = fmaf(w, q.inv_h, q.c1);
-            const float4 qa = Ml[k].a;
-            const float2 qb = Ml[k].b;
             const float t1 = fmaf(nu1, nu1, 1.0f);
             const float rs = rsqrtf(fmaf(-pc.g2, nu1, pc.g1));
             const float rs3 = rs * rs * rs;
-            inc.x = fmaf(fmaf(qa.w, w, qa.x), rs3, inc.x) * t1;
-            inc.y = fmaf(fmaf(qb.x, w, qa.y), rs3, inc.y) * t1;
-            inc.z = fmaf(fmaf(qb.y, w, qa.z), rs3, inc.z) * t1;
+            inc.x = fmaf(fmaf(rc.y, w, rb.z), rs3, fmaf(ra.w, w, ra.x)) * t1;
+            inc.y = fmaf(fmaf(rc.z, w, rb.w), rs3, fmaf(rb.x, w, ra.y)) * t1;
+            inc.z = fmaf(fmaf(rc.w, w, rc.x), rs3, fmaf(rb.y, w, ra.z)) * t1;
           }
           if (GROUND) {
             // irradiance of order n - 2 where omega_i meets the ground
@@ -1046,14 +1057,13 @@ __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned cha
   __syncthreads();
   // --- reduced tables: the previous order's table at this tile's r and mu_s
   // columns, on the theta rows, as nu intervals: the entries (pass 1), the
-  // differences (pass 2, into b and pad, which pass 1 readers do not touch),
+  // differences (pass 2, into the slope fields, which pass 2 readers do not touch),
   // then the line's value at w = 0 and its slope in place (pass 3); the same
   // for the ground irradiance row; direction pairs with ground normals,
   // pre-scaled for line_pos
   const int MK = dens_mk(NNU, CL), MKE = dens_mke(a.ir_mus, CL);
-  const size_t nPtab = (size_t)sh.S * NT * MK;
   const int per_col = NT * MK;
-  const int ntab = TWO ? 2 : 1;
+  LerpRec2* const P2 = reinterpret_cast<LerpRec2*>(S.P);  // order 2
   const float hP = 0.5f * float(NNU - 1), hE = 0.5f * float(a.ir_mus - 1);
   {
     const float4* src0 = TWO ? a.dr : a.dms;
@@ -1072,11 +1082,13 @@ __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned cha
         v = fetch3(src0, a.W, a.sc_mu, S.kax[c * NK + sl], S.tay[l], s_az) * sR;
         if (TWO) m = fetch3(a.dm, a.W, a.sc_mu, S.kax[c * NK + sl], S.tay[l], s_az) * sM;
       }
-      S.P[k].a = make_float4(v.x, v.y, v.z, 0.f);
-      S.P[k].b = S.P[k].pad = make_float2(0.f, 0.f);
-      if (TWO) {
-        S.P[nPtab + k].a = make_float4(m.x, m.y, m.z, 0.f);
-        S.P[nPtab + k].b = S.P[nPtab + k].pad = make_float2(0.f, 0.f);
+      if (!TWO) {
+        S.P[k].a = make_float4(v.x, v.y, v.z, 0.f);
+        S.P[k].b = S.P[k].pad = make_float2(0.f, 0.f);
+      } else {
+        P2[k].a = make_float4(v.x, v.y, v.z, 0.f);
+        P2[k].b = make_float4(0.f, 0.f, m.x, m.y);
+        P2[k].c = make_float4(m.z, 0.f, 0.f, 0.f);
       }
     }
     const float dtheta = kPiF / float(NT), dphi = kPiF / float(NT);
@@ -1115,10 +1127,20 @@ __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned cha
       const int p = k % MK, row0 = k - p, ki = rec_interval<CL>(p, MK);
       if (ki <= NNU - 1) {  // intervals -1 .. nu_size - 1
         const int right = row0 + rec_pos<CL>(ki + 1, MK);
-        for (int tb = 0; tb < ntab; ++tb) {
-          const float4 v0 = S.P[tb * nPtab + k].a, v1 = S.P[tb * nPtab + right].a;
-          S.P[tb * nPtab + k].b = make_float2(v1.x - v0.x, v1.y - v0.y);
-          S.P[tb * nPtab + k].pad = make_float2(v1.z - v0.z, 0.f);
+        if (!TWO) {
+          const float4 v0 = S.P[k].a, v1 = S.P[right].a;
+          S.P[k].b = make_float2(v1.x - v0.x, v1.y - v0.y);
+          S.P[k].pad = make_float2(v1.z - v0.z, 0.f);
+        } else {
+          // values only (the slope slots of `right` are being written by its owner)
+          LerpRec2& r0 = P2[k];
+          const LerpRec2& r1 = P2[right];
+          r0.a.w = r1.a.x - r0.a.x;
+          r0.b.x = r1.a.y - r0.a.y;
+          r0.b.y = r1.a.z - r0.a.z;
+          r0.c.y = r1.b.z - r0.b.z;
+          r0.c.z = r1.b.w - r0.b.w;
+          r0.c.w = r1.c.x - r0.c.x;
         }
       }
     }
@@ -1139,9 +1161,20 @@ __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned cha
       rec.a = make_float4(fmaf(c, d.x, rec.a.x), fmaf(c, d.y, rec.a.y), fmaf(c, d.z, rec.a.z), d.x);
       rec.b = make_float2(d.y, d.z);
     };
-    for (int k = tid; k < ntab * ns * per_col; k += nth) {
-      const int kk = k % (ns * per_col);
-      line(S.P[(k / (ns * per_col)) * nPtab + kk], rec_interval<CL>(kk % MK, MK));
+    for (int k = tid; k < ns * per_col; k += nth) {
+      const int ki = rec_interval<CL>(k % MK, MK);
+      if (!TWO) {
+        line(S.P[k], ki);
+      } else {
+        LerpRec2& r = P2[k];
+        const float c = 0.5f - float(ki);
+        r.a.x = fmaf(c, r.a.w, r.a.x);
+        r.a.y = fmaf(c, r.b.x, r.a.y);
+        r.a.z = fmaf(c, r.b.y, r.a.z);
+        r.b.z = fmaf(c, r.c.y, r.b.z);
+        r.b.w = fmaf(c, r.c.z, r.b.w);
+        r.c.x = fmaf(c, r.c.w, r.c.x);
+      }
     }
     for (int k = tid; k < MKE; k += nth) line(S.E[k], rec_interval<CL>(k, MKE));
   }
@@ -1232,12 +1265,13 @@ __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned cha
     }
     for (int l = 0; l < NT; ++l) {
       const DensTheta t = S.th[l];
-      const LerpRec* Pl = S.P + (size_t)(cl * NT + l) * MK;
-      const LerpRec* Ml = Pl + nPtab;
+      const size_t row = (size_t)(cl * NT + l) * MK;
+      const LerpRec* Pl = TWO ? reinterpret_cast<const LerpRec*>(reinterpret_cast<const LerpRec2*>(S.P) + row)
+                              : S.P + row;
       if (t.ground)
-        dens_row<TWO, true, CL>(S, t, l, NT, Pl, Ml, q, sx, sy, G, pc, acc);
+        dens_row<TWO, true, CL>(S, t, l, NT, Pl, q, sx, sy, G, pc, acc);
       else
-        dens_row<TWO, false, CL>(S, t, l, NT, Pl, Ml, q, sx, sy, G, pc, acc);
+        dens_row<TWO, false, CL>(S, t, l, NT, Pl, q, sx, sy, G, pc, acc);
       if (MX && ((l + 1) % kDensKahanRows == 0 || l == NT - 1)) {
         // Kahan sum over theta rows of the FP32 sums over kDensKahanRows rows
 #pragma unroll
