@@ -287,7 +287,22 @@ struct Kahan3 {
     add1(s.y, c.y, v.y);
     add1(s.z, c.z, v.z);
   }
+  // add(u * v) with the product formed inside the first FMA (unrounded)
+  __device__ __forceinline__ static void add1_prod(float& sum, float& comp, float u, float v) {
+    float y = fmaf(u, v, -comp);
+    float t = sum + y;
+    comp = (t - sum) - y;
+    sum = t;
+  }
+  __device__ __forceinline__ void add_prod(float3 u, float3 v) {
+    add1_prod(s.x, c.x, u.x, v.x);
+    add1_prod(s.y, c.y, u.y, v.y);
+    add1_prod(s.z, c.z, u.z, v.z);
+  }
 };
+__device__ __forceinline__ float3 fma3(float3 a, float3 b, float3 c) {
+  return make_float3(fmaf(a.x, b.x, c.x), fmaf(a.y, b.y, c.y), fmaf(a.z, b.z, c.z));
+}
 
 __device__ __forceinline__ float store_round(float v, int f16) {
   return f16 ? __half2float(__float2half_rn(v)) : v;
@@ -587,14 +602,18 @@ struct MuS32 {
     inv_A = a.mus_inv_A;
     scale = float(a.sc_mus - 1);
   }
-  // texel coordinate within a nu slice
+  // texel coordinate within a nu slice. The distance to the top is d = P / Q
+  // (rationalised where the ray points up); with a = (d - dmin) / span the
+  // coordinate max(1 - a / A, 0) / (1 + a) is formed as one quotient,
+  // max(Q - a Q / A, 0) / (Q + a Q).
   __device__ __forceinline__ float texel(float mu_s) const {
     float s = R * mu_s;
     const float disc = fmaf(s, s, H2);  // >= H^2 > 0
     float root = disc * rsqrtf(disc);
-    float d = s > 0.0f ? __fdividef(H2, s + root) : root - s;
-    float aa = (d - dmin) * inv_span;
-    return __fdividef(gmax(1.0f - aa * inv_A, 0.0f), 1.0f + aa) * scale;
+    const bool up = s > 0.0f;
+    const float P = up ? H2 : root - s, Q = up ? s + root : 1.0f;
+    const float aQ = fmaf(-dmin, Q, P) * inv_span;
+    return __fdividef(gmax(fmaf(-aQ, inv_A, Q), 0.0f), Q + aQ) * scale;
   }
 };
 

@@ -706,13 +706,13 @@ __device__ void tile_single(const DevAtmo& a, int tile, unsigned char* smem) {
       ay.i1 = o.y1;
       ay.f = o.fy;
       const float3 ts = fetch2_pairs(a.trp, a.tr_mu, ax, ay) * sfac;
-      const float3 ri_ = ts * make_float3(o.trx, o.try_, o.trz), mi_ = ts * make_float3(o.tmx, o.tmy, o.tmz);
+      const float3 tr3 = make_float3(o.trx, o.try_, o.trz), tm3 = make_float3(o.tmx, o.tmy, o.tmz);
       if (!MX) {
-        ray.s = ray.s + ri_;
-        mie.s = mie.s + mi_;
+        ray.s = fma3(ts, tr3, ray.s);
+        mie.s = fma3(ts, tm3, mie.s);
       } else {
-        ray.add(ri_);
-        mie.add(mi_);
+        ray.add_prod(ts, tr3);
+        mie.add_prod(ts, tm3);
       }
     }
     const float dx = MX ? (float)(ri.distd / double(N)) : ri.dist / float(N);
@@ -1685,12 +1685,12 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
         const float ay = fmaf(sg[1] - sg[0], fx, sg[0]), by = fmaf(sg[NM + 1] - sg[NM], fx, sg[NM]);
         const float az = fmaf(sb[1] - sb[0], fx, sb[0]), bz = fmaf(sb[NM + 1] - sb[NM], fx, sb[NM]);
         const float3 J = make_float3(fmaf(bx - ax, lf, ax), fmaf(by - ay, lf, ay), fmaf(bz - az, lf, az));
-        const float3 v = J * make_float3(o.tvwx, o.tvwy, o.tvwz);
+        const float3 tvw = make_float3(o.tvwx, o.tvwy, o.tvwz);
         if (!MX) {
-          acc[j].s = acc[j].s + v;
+          acc[j].s = fma3(J, tvw, acc[j].s);
         } else {
           // plain sums over runs of 8 samples, Kahan-compensated across runs
-          part[j] = part[j] + v;
+          part[j] = fma3(J, tvw, part[j]);
           if ((i & 7) == 7 || i == N) {
             acc[j].add(part[j]);
             part[j] = make_float3(0.f, 0.f, 0.f);
