@@ -690,7 +690,10 @@ __device__ void tile_single(const DevAtmo& a, int tile, unsigned char* smem) {
         // under the root, rationalised when the ray points up.
         float s_d = gclamp(fmaf(o.d, nu, r_mu_s), -o.r_d, o.r_d);
         mu_s_d = s_d * o.inv_r;
-        float root = sqrtf(fmaf(s_d, s_d, o.e));
+        // square root as x rsqrt(x) (a few ulp; 0 where the argument is 0,
+        // on the top boundary)
+        const float disc = fmaf(s_d, s_d, o.e);
+        const float root = disc > 0.0f ? disc * rsqrtf(disc) : 0.0f;
         float dt = s_d > 0.0f ? __fdividef(o.e, s_d + root) : root - s_d;
         x_mu = (dt - o.dmin) * o.inv_span;
       }
