@@ -49,10 +49,19 @@ class DeviceArray:
         return t.cpu().numpy()
 
 
+def planes_to_rgba(planes: np.ndarray, width: int) -> np.ndarray:
+    """(depth, height, 3, stride) float planes -> (depth, height, width, 4) RGBA
+    with alpha 0 (the layout scattering_density.comp:155 writes)."""
+    p = planes[..., :width]
+    out = np.zeros(p.shape[:2] + (width, 4), np.float32)
+    out[..., :3] = np.moveaxis(p, 2, 3)
+    return out
+
+
 class PlanarDensity(DeviceArray):
     """The scattering-density temporary, stored as three float planes (R, G, B)
     per (r, mu) row of `stride` floats; to_numpy() gives the RGBA layout of the
-    other scattering-class tables (alpha 0, as scattering_density.comp:155 writes)."""
+    other scattering-class tables."""
 
     def __init__(self, ptr: int, extent, stride: int, owner=None):
         sd, sh, sw = extent
@@ -60,10 +69,7 @@ class PlanarDensity(DeviceArray):
         self.width = int(sw)
 
     def to_numpy(self) -> np.ndarray:
-        planes = super().to_numpy()[..., :self.width]
-        out = np.zeros(planes.shape[:2] + (self.width, 4), np.float32)
-        out[..., :3] = np.moveaxis(planes, 2, 3)
-        return out
+        return planes_to_rgba(super().to_numpy(), self.width)
 
 
 class Builder:

@@ -134,3 +134,30 @@ def test_rust_sys_params_layout_matches_header():
         rb = re.search(r"pub struct %s \{(.*?)\n\}" % name, rust, re.S).group(1)
         rf = re.findall(r"pub (\w+):", rb)
         assert hf == rf, (name, hf, rf)
+
+
+def test_intermediates_struct_matches_bindings():
+    """fb_intermediates: the Python ctypes struct and the Rust struct list the
+    header's fields in its order."""
+    import re
+    from fuzzyblue_gb300 import _native as N
+    header = open(os.path.join(ROOT, "include", "fuzzyblue.h")).read()
+    hb = re.search(r"typedef struct fb_intermediates \{(.*?)\} fb_intermediates;", header, re.S).group(1)
+    hb = re.sub(r"/\*.*?\*/", "", hb, flags=re.S)
+    hf = re.findall(r"\b(?:void\*|uint32_t)\s+(\w+)", hb)
+    assert hf == [f[0] for f in N.c_intermediates._fields_]
+    rb = re.search(r"pub struct fb_intermediates \{(.*?)\n\}", _rust_sys(), re.S).group(1)
+    assert hf == re.findall(r"pub (\w+):", rb)
+
+
+def test_planar_density_to_rgba():
+    """The planar density temporary (R, G, B planes of `stride` floats per
+    (r, mu) row) reads back as the RGBA layout of the other tables."""
+    from fuzzyblue_gb300.api import planes_to_rgba
+    depth, height, width, stride = 2, 3, 5, 8
+    rng = np.random.default_rng(0)
+    rgba = rng.random((depth, height, width, 4), dtype=np.float32)
+    rgba[..., 3] = 0.0
+    planes = np.full((depth, height, 3, stride), np.nan, np.float32)  # padding never read
+    planes[..., :width] = np.moveaxis(rgba[..., :3], 3, 2)
+    assert np.array_equal(planes_to_rgba(planes, width), rgba)
