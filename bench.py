@@ -194,7 +194,7 @@ def run_ours(a):
         import torch.distributed as td
         td.init_process_group("nccl")
     from fuzzyblue_gb300 import workloads
-    from fuzzyblue_gb300.api import Atmosphere, Builder, build_batch
+    from fuzzyblue_gb300.api import Atmosphere, Builder, build_batch, device_bytes
     from fuzzyblue_gb300.params import PRECISION_MIXED, PRECISION_PLAIN, Parameters
 
     builder = Builder(local)
@@ -380,7 +380,7 @@ def run_ours(a):
                    "batch_per_gpu": a.batch, "orders": ORDERS, "precision": a.precision,
                    "parallelism": "replicas" if world > 1 else "single",
                    "l2": "inputs larger than L2: ~%d GB of tables and temporaries per step" % round(
-                       a.batch * 0.1)},
+                       sum(sum(device_bytes(p)) for p in params) / 1e9)},
         "clocks": clk,
         "e2e": {"value": e2e, "unit": "atmospheres/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": a.batch * per_atm,
