@@ -1002,7 +1002,7 @@ __device__ __forceinline__ void dens_row(const DensLayout& S, const DensTheta& t
 }
 
 // MIXED density: theta rows summed in FP32 between two Kahan steps.
-constexpr int kDensKahanRows = 2;
+constexpr int kDensKahanRows = 4;
 
 // One Kahan step on a (sum, compensation) pair held in shared memory. The
 // pointers are volatile so that the compiler keeps the pair in shared memory
