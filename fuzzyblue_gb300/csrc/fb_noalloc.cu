@@ -20,6 +20,13 @@
 // call on a device sets that device up (looks up the scratch address and
 // raises the kernels' shared-memory limits); make that first call before any
 // stream capture.
+//
+// Every check (parameters, scratch size, each launch's shared memory and
+// occupancy) runs before anything is enqueued, so a call that returns an error
+// has enqueued nothing and left the output tables and the scratch untouched.
+// The per-atmosphere record and the work lists are written on the device by a
+// small kernel from its launch arguments: a call copies nothing from host
+// memory.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -36,8 +43,25 @@ namespace {
 
 constexpr size_t kNoAllocScratchBytes = 16u << 20;
 constexpr int kMaxDevices = 64;
+constexpr int kMaxLaunches = 2 + 2 * 64;                       // T, S, then D and M for orders 2..64
+constexpr int kNumInts = 2 * fb::kMaxSegments * kMaxLaunches;  // per launch and segment: a job id, an offset
 
 static __device__ __align__(256) unsigned char g_scratch[kNoAllocScratchBytes];
+
+// The record travels as a launch argument (copied by the launch itself).
+static_assert(sizeof(fb::DevAtmo) <= 4000, "the atmosphere record must fit in a kernel's arguments");
+
+// Writes the atmosphere record into the scratch and clears the work lists (one
+// job, id 0, at offset 0) and the launches' work counters.
+__global__ void k_noalloc_prepare(fb::DevAtmo d, fb::DevAtmo* dst, int* ints, unsigned* counters) {
+  const int t = threadIdx.x;
+  const int* src = reinterpret_cast<const int*>(&d);
+  int* out = reinterpret_cast<int*>(dst);
+  for (int i = t; i < (int)(sizeof(fb::DevAtmo) / sizeof(int)); i += blockDim.x) out[i] = src[i];
+  for (int i = t; i < kNumInts; i += blockDim.x) ints[i] = 0;
+  for (int i = t; i < kMaxLaunches; i += blockDim.x) counters[i] = 0u;
+}
+static_assert(sizeof(fb::DevAtmo) % sizeof(int) == 0, "the record is copied as ints");
 
 struct DeviceSetup {
   bool done = false;
@@ -51,7 +75,9 @@ DeviceSetup g_setup[kMaxDevices];
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
-// Once per device, with that device current.
+// Once per device, with that device current: the scratch address and every
+// pass kernel's dynamic shared-memory limit (the same kernels the builder sets
+// up: variants 0..5, of order 2 or not).
 int setup_device(int dev, DeviceSetup** out) {
   std::lock_guard<std::mutex> g(g_setup_mu);
   DeviceSetup& d = g_setup[dev];
@@ -70,17 +96,16 @@ int setup_device(int dev, DeviceSetup** out) {
     for (int mode = 0; mode < 2; ++mode)
       for (int pass = 0; pass < 4; ++pass)
         for (int tpt : {1, 2})
-          for (int variant : {0, 2, fb::kDensClamped, 10, 12, 10 + fb::kDensClamped}) {
-          // variants 0, 2 and clamped density tables, of order 2 (+ 10) or not
-          const void* k = fb::kernel_for(mode == 1, pass, tpt, variant % 10, variant >= 10);
-          cudaFuncAttributes fa;
-          if (cudaFuncGetAttributes(&fa, k) != cudaSuccess ||
-              cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)prop.sharedMemPerBlockOptin - (int)fa.sharedSizeBytes) != cudaSuccess) {
-            cudaGetLastError();
-            return fbi::set_error(FB_ERR_NO_KERNEL, "no sm_103a kernel image loads on this device");
+          for (int variant = 0; variant < 12; ++variant) {
+            const void* k = fb::kernel_for(mode == 1, pass, tpt, variant % 6, variant >= 6);
+            cudaFuncAttributes fa;
+            if (cudaFuncGetAttributes(&fa, k) != cudaSuccess ||
+                cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)prop.sharedMemPerBlockOptin - (int)fa.sharedSizeBytes) != cudaSuccess) {
+              cudaGetLastError();
+              return fbi::set_error(FB_ERR_NO_KERNEL, "no sm_103a kernel image loads on this device");
+            }
           }
-        }
     d.scratch = static_cast<unsigned char*>(ptr);
     d.sms = prop.multiProcessorCount;
     d.smem_optin = (int)prop.sharedMemPerBlockOptin;
@@ -90,12 +115,13 @@ int setup_device(int dev, DeviceSetup** out) {
   return FB_OK;
 }
 
+// A launch with its grid decided and its checks passed.
 struct Launch {
   const void* fn;
   fb::LaunchArgs args;
+  int grid;
   int block;
   size_t smem;
-  int total;
 };
 
 }  // namespace
@@ -121,15 +147,13 @@ extern "C" int fb_atmosphere_build_noalloc(void* stream, const fb_params* p, voi
   // layout of the scratch: record, work lists, counters, temporaries
   const fbi::TableSizes z = fbi::sizes_of(*p);
   const bool mixed = p->precision == FB_PRECISION_MIXED;
-  const int max_launches = 2 + 2 * 64;
-  const int n_ints = 2 * fb::kMaxSegments * max_launches;  // per launch and segment: one job id, one offset
   size_t off = 0;
   const size_t o_atm = off;
   off = align256(off + sizeof(fb::DevAtmo));
   const size_t o_ints = off;
-  off = align256(off + sizeof(int) * n_ints);
+  off = align256(off + sizeof(int) * kNumInts);
   const size_t o_cnt = off;
-  off = align256(off + sizeof(unsigned) * max_launches);
+  off = align256(off + sizeof(unsigned) * kMaxLaunches);
   const size_t o_tmp = off;
   off += z.tmp_bytes;
   if (off > kNoAllocScratchBytes) {
@@ -160,13 +184,19 @@ extern "C" int fb_atmosphere_build_noalloc(void* stream, const fb_params* p, voi
     char* gp = (char*)tp;
     fbi::place_geometry(d, gp, mixed);
   }
-  // launches of the pass order (src/precompute.rs:1726-1999), one job each
-  std::vector<int> ints(n_ints, 0);  // job ids 0, offsets 0
-  const fb::DevAtmo* d_atm = (const fb::DevAtmo*)(base + o_atm);
-  const int* d_ints = (const int*)(base + o_ints);
+  fb::DevAtmo* d_atm = (fb::DevAtmo*)(base + o_atm);
+  int* d_ints = (int*)(base + o_ints);
   unsigned* d_cnt = (unsigned*)(base + o_cnt);
+
+  // launches of the pass order (src/precompute.rs:1726-1999), one job each;
+  // launch k uses work counter k and work-list ints [2 kMaxSegments k, ...).
+  // Each is checked and its grid decided here; launches without work items
+  // (order 1 has none after the first two) are left out.
   std::vector<Launch> L;
-  auto add = [&](int pass, int order, std::vector<int> tiles, size_t smem, int tpt, int block, int variant) {
+  int slot = 0;
+  auto add = [&](int pass, int order, std::vector<int> tiles, size_t smem, int tpt, int block,
+                 int variant) -> int {
+    const int k = slot++;
     Launch l;
     std::memset(&l, 0, sizeof(l));
     l.fn = fb::kernel_for(mixed, pass, tpt, variant, order == 2);
@@ -175,55 +205,62 @@ extern "C" int fb_atmosphere_build_noalloc(void* stream, const fb_params* p, voi
     l.args.atm = d_atm;
     l.args.nseg = (int)tiles.size();
     l.args.order = order;
-    l.args.counter = d_cnt + L.size();
-    l.total = 0;
+    l.args.counter = d_cnt + k;
+    int total = 0;
     for (int sgi = 0; sgi < (int)tiles.size(); ++sgi) {
-      const size_t at = 2 * (fb::kMaxSegments * L.size() + sgi);
+      const size_t at = 2 * (fb::kMaxSegments * (size_t)k + sgi);
       l.args.seg[sgi].njobs = 1;
       l.args.seg[sgi].total = tiles[sgi];
       l.args.seg[sgi].job = d_ints + at;
       l.args.seg[sgi].off = d_ints + at + 1;
-      l.total += tiles[sgi];
+      total += tiles[sgi];
     }
+    if (total == 0) return FB_OK;
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, l.fn) != cudaSuccess) {
+      cudaGetLastError();
+      return fbi::set_error(FB_ERR_CUDA, "cudaFuncGetAttributes failed");
+    }
+    if ((int)(l.smem + fa.sharedSizeBytes) > ds->smem_optin)
+      return fbi::set_error(FB_ERR_INVALID_PARAMS, "shared memory of a pass exceeds the device limit");
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, l.fn, l.block, l.smem) != cudaSuccess || per_sm < 1) {
+      cudaGetLastError();
+      return fbi::set_error(FB_ERR_CUDA, "occupancy query failed: a pass cannot be resident on this device");
+    }
+    l.grid = std::max(1, std::min(total, per_sm * ds->sms));
     L.push_back(l);
+    return FB_OK;
   };
   const bool multi = d.order >= 2;
-  add(fb::kPassTransmittance, 0,
-      {fb::tiles_transmittance(d.tr_mu, d.tr_r),
-       fb::tiles_geometry(d.W, d.sc_mu, d.sc_r, mixed ? fb::irgeo_entries(d.ir_r, d.ir_mus, d.irr_n, d.sc_nu) : 0)},
-      0, 1, fb::kThreads, 0);
-  add(fb::kPassSingle, 0,
-      {fb::tiles_rows(d.W, d.sc_mu, d.sc_r), fb::tiles_direct(d.ir_mus, d.ir_r),
-       multi ? fb::tiles_msrec(d.sc_mu, d.sc_r, d.ms_steps) : 0, multi ? fb::tiles_densgeo(d.sc_r, d.dens_n) : 0},
-      fb::ss_smem(d.W, d.ss_steps, d.sc_mus, d.sc_nu), 1, fb::kThreads, 0);
+  rc = add(fb::kPassTransmittance, 0,
+           {fb::tiles_transmittance(d.tr_mu, d.tr_r),
+            fb::tiles_geometry(d.W, d.sc_mu, d.sc_r, mixed ? fb::irgeo_entries(d.ir_r, d.ir_mus, d.irr_n, d.sc_nu) : 0)},
+           0, 1, fb::kThreads, 0);
+  if (!rc)
+    rc = add(fb::kPassSingle, 0,
+             {fb::tiles_rows(d.W, d.sc_mu, d.sc_r), fb::tiles_direct(d.ir_mus, d.ir_r),
+              multi ? fb::tiles_msrec(d.sc_mu, d.sc_r, d.ms_steps) : 0, multi ? fb::tiles_densgeo(d.sc_r, d.dens_n) : 0},
+             fb::ss_smem(d.W, d.ss_steps, d.sc_mus, d.sc_nu), 1, fb::kThreads, 0);
   const int ms_block = fb::ms_threads(d.W);
-  for (int n = 2; n <= d.order; ++n) {
+  for (int n = 2; !rc && n <= d.order; ++n) {
     const bool cl = fb::density_smem(d, n == 2, mixed, false) > (size_t)std::max(0, ds->smem_optin - 1024);
     const size_t sm = std::max(fb::density_smem(d, n == 2, mixed, cl), fb::indirect_smem(d.irr_n, d.sc_nu, n - 1 == 1));
-    add(fb::kPassDensity, n, {fb::tiles_density(d), fb::tiles_indirect(d.ir_mus, d.ir_r)}, sm, 1, fb::kDensThreads,
-        cl ? fb::kDensClamped : 0);
-    add(fb::kPassMultiple, n, {fb::tiles_multiple(d.W, d.sc_mus, d.ms_steps, d.sc_mu, d.sc_r, ms_block)},
-        fb::ms_smem(d.W, d.ms_steps, d.sc_mus, ms_block), fb::ms_shape(d.W, d.sc_mus, d.ms_steps, ms_block).TPT, ms_block,
-        std::max(0, fb::ms_block_variant(ms_block)));
+    rc = add(fb::kPassDensity, n, {fb::tiles_density(d), fb::tiles_indirect(d.ir_mus, d.ir_r)}, sm, 1,
+             fb::kDensThreads, cl ? fb::kDensClamped : 0);
+    if (!rc)
+      rc = add(fb::kPassMultiple, n, {fb::tiles_multiple(d.W, d.sc_mus, d.ms_steps, d.sc_mu, d.sc_r, ms_block)},
+               fb::ms_smem(d.W, d.ms_steps, d.sc_mus, ms_block), fb::ms_shape(d.W, d.sc_mus, d.ms_steps, ms_block).TPT,
+               ms_block, std::max(0, fb::ms_block_variant(ms_block)));
   }
-  cudaError_t e = cudaMemcpyAsync(base + o_atm, &d, sizeof(d), cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(base + o_ints, ints.data(), sizeof(int) * n_ints, cudaMemcpyHostToDevice, st);
-  // the work counters are the only scratch that must start at zero
-  if (e == cudaSuccess) e = cudaMemsetAsync(d_cnt, 0, sizeof(unsigned) * L.size(), st);
+  if (rc) return rc;
+
+  // enqueue: the record and cleared work lists, then the passes
+  void* pargs[] = {(void*)&d, (void*)&d_atm, (void*)&d_ints, (void*)&d_cnt};
+  cudaError_t e = cudaLaunchKernel((const void*)k_noalloc_prepare, dim3(1), dim3(256), pargs, 0, st);
   for (size_t k = 0; e == cudaSuccess && k < L.size(); ++k) {
-    cudaFuncAttributes fa;
-    e = cudaFuncGetAttributes(&fa, L[k].fn);
-    if (e != cudaSuccess) break;
-    if ((int)(L[k].smem + fa.sharedSizeBytes) > ds->smem_optin) {
-      return fbi::set_error(FB_ERR_INVALID_PARAMS, "shared memory of a pass exceeds the device limit");
-    }
-    int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, L[k].fn, L[k].block, L[k].smem);
-    if (e != cudaSuccess) break;
-    const int grid = std::max(1, std::min(L[k].total, std::max(per_sm, 1) * ds->sms));
     void* args[] = {(void*)&L[k].args};
-    e = cudaLaunchKernel(L[k].fn, dim3(grid), dim3(L[k].block), args, L[k].smem, st);
+    e = cudaLaunchKernel(L[k].fn, dim3(L[k].grid), dim3(L[k].block), args, L[k].smem, st);
   }
   if (e != cudaSuccess) {
     const char* m = cudaGetErrorString(e);

@@ -4,10 +4,12 @@
   oracle/_ref/libfbref.so        the reference's own shaders compiled as C++
                                  (ref_glsl/translate.py + glsl_shim.hpp + ref_runner.cpp)
 
-The reference build reads the shader sources from the reference checkout
-(FB_REFERENCE_DIR, default /root/reference) when it is present and writes the
-rewritten sources to oracle/_ref/gen/; where the checkout is absent but the
-rewritten sources are, it compiles those. Both outputs are git-ignored.
+The reference build reads the shader sources from the reference checkout when
+it is present and writes the rewritten sources to oracle/_ref/gen/; where the
+checkout is absent but the rewritten sources are, it compiles those. Both
+outputs are git-ignored. The checkout is FB_REFERENCE_DIR if set, else the
+path in oracle/reference_dir.txt, relative to the repository root (a sibling
+checkout named `reference`).
 """
 import os
 import subprocess
@@ -48,20 +50,31 @@ def build_oracle(force=False):
 
 
 def reference_dir():
-    return os.environ.get("FB_REFERENCE_DIR", "/root/reference")
+    """The reference checkout, or None when none is configured."""
+    env = os.environ.get("FB_REFERENCE_DIR")
+    if env:
+        return env
+    cfg = os.path.join(HERE, "reference_dir.txt")
+    if os.path.exists(cfg):
+        with open(cfg) as f:
+            rel = f.read().strip()
+        if rel:
+            return os.path.normpath(os.path.join(ROOT, rel))
+    return None
 
 
 def build_reference(force=False):
     """Returns the path of libfbref.so, or None when neither the reference
     checkout nor previously rewritten sources are available."""
     gen = os.path.join(REF_DIR, "gen")
-    shaders = os.path.join(reference_dir(), "shaders")
+    ref = reference_dir()
+    shaders = os.path.join(ref, "shaders") if ref else None
     sys.path.insert(0, os.path.join(HERE, "ref_glsl"))
     try:
         import translate  # noqa: E402
     finally:
         sys.path.pop(0)
-    if os.path.isdir(shaders):
+    if shaders and os.path.isdir(shaders):
         translate.main(["--shaders", shaders, "--out", gen])
     if not all(os.path.exists(os.path.join(gen, n)) for n in translate.HEADERS + translate.PASSES + translate.RENDER):
         return None

@@ -1,0 +1,175 @@
+"""GPU parity on the benchmarked configurations themselves.
+
+1. The headline's own atmospheres: the first 8 draws of the uniform batch
+   (workloads.uniform_batch(256, seed=0)) and, from the same 256 draws, the one
+   with the smallest planet (index 95, bottom radius 3001 km), the thinnest
+   atmosphere (index 216, 40.7 km) and the largest Mie coefficient (index 161).
+   At the default table sizes in MIXED precision, every pass of the GPU against
+   the FP64 oracle's same pass on the GPU's own inputs (sampled texels, as in
+   test_parity_gpu.test_each_pass_at_default_size); at the sizes of the crate's
+   dump example (r16 mu64 mu_s16 nu4, 4 orders) the whole precompute against
+   the FP64 oracle on every texel.
+2. Orders 5-8 (the uneven and serving workloads draw orders in 2-8; the
+   reference's order loop, src/precompute.rs:1853-1999, accumulates every
+   order into the scattering and irradiance tables,
+   multiple_scattering.comp:91-92, indirect_irradiance.comp:72-73): the whole
+   precompute at the smoke and dump sizes, MIXED against FP64 and PLAIN
+   against the FP32 oracle.
+3. 4x resolution (the precision configuration: TR 512x128 / 2000 steps, IR
+   128x32, SC r64 mu256 mu_s64 nu16, 8 orders): the order-8 density, the
+   order-7 indirect irradiance and the order-8 multiple scattering against
+   FP64, fed the GPU's order-7 inputs (the whole FP64 precompute at this size
+   is out of reach of the CPU oracle).
+
+Tolerances: MIXED max 1e-3 relative against FP64 (the target); PLAIN max 2e-3,
+RMS 1e-4 against the FP32 oracle (whole precompute). Relative error with the
+floor 1e-6 * max|ref| (tests/errors.py). Each check prints a line starting
+with PARITY (pytest -s) with the max and RMS per LUT or pass.
+"""
+import numpy as np
+import pytest
+
+from fuzzyblue_gb300 import workloads
+from fuzzyblue_gb300.params import PRECISION_MIXED, Parameters, dump_parameters, smoke_parameters
+from tests.errors import summary
+
+pytestmark = pytest.mark.gpu
+
+MIXED_MAX = 1e-3
+PLAIN_MAX, PLAIN_RMS = 2e-3, 1e-4
+HEADLINE = list(range(8)) + [95, 216, 161]
+KEYS = ("transmittance", "irradiance", "scattering")
+
+
+def _draws():
+    return workloads.uniform_batch(256, seed=0)
+
+
+def _build(builder, p, intermediates=False):
+    from fuzzyblue_gb300.api import Atmosphere
+    pend = Atmosphere.build(builder, p)
+    pend.wait()
+    pend.assert_ready()
+    out = pend.atmosphere().to_host()
+    if intermediates:
+        out.update({k: v.to_numpy() for k, v in pend.intermediates().items()})
+    pend.release()
+    return out
+
+
+def _report(tag, name, s):
+    print("PARITY %s | %s | max %.3e rms %.3e p99.9 %.3e" % (tag, name, s["max"], s["rms"], s["p999"]))
+
+
+def _check64(tag, name, got, ref):
+    got = np.asarray(got)
+    assert np.isfinite(got).all(), (tag, name)
+    s = summary(got.astype(np.float64), ref)
+    _report(tag, name, s)
+    assert s["max"] <= MIXED_MAX, (tag, name, s)
+
+
+def _flat(a):
+    return np.ascontiguousarray(a.reshape(-1, 4))
+
+
+def _passes_vs_fp64(builder, oracle, p, tag, samples=512):
+    """Orders 2 and 3 of a MIXED build: every pass against the FP64 oracle."""
+    f64 = np.float64
+    rng = np.random.default_rng(11)
+    ntr, nir, nsc = p.texel_counts()
+    o2 = _build(builder, p.replace(order=2), intermediates=True)
+    o3 = _build(builder, p.replace(order=3), intermediates=True)
+    tr = _flat(o2["transmittance"]).astype(f64)
+    idx = np.sort(rng.choice(ntr, min(ntr, 1024), replace=False)).astype(np.int64)
+    _check64(tag, "transmittance", tr[idx], oracle.transmittance(p, idx, dtype=f64))
+    d0 = _flat(o2["delta_irradiance_0"]).astype(f64)
+    _check64(tag, "direct irradiance", d0, oracle.direct_irradiance(p, tr, dtype=f64))
+    dr, dm = _flat(o2["delta_rayleigh"]).astype(f64), _flat(o2["delta_mie"]).astype(f64)
+    idx = np.sort(rng.choice(nsc, samples * 2, replace=False)).astype(np.int64)
+    r, m = oracle.single_scattering(p, tr, idx=idx, dtype=f64)
+    _check64(tag, "single rayleigh", dr[idx], r)
+    _check64(tag, "single mie", dm[idx], m)
+    idx = np.sort(rng.choice(nsc, samples, replace=False)).astype(np.int64)
+    dens2 = _flat(o2["scattering_density"]).astype(f64)
+    _check64(tag, "density order 2", dens2[idx],
+             oracle.scattering_density(p, 2, tr, dr, dm, None, d0, idx=idx, dtype=f64))
+    e1 = _flat(o2["delta_irradiance_1"]).astype(f64)
+    _check64(tag, "indirect order 1", e1, oracle.indirect_irradiance(p, 1, dr, dm, None, dtype=f64))
+    ms2 = _flat(o2["delta_multiple_scattering"]).astype(f64)
+    ref, _ = oracle.multiple_scattering(p, tr, dens2, idx=idx, dtype=f64)
+    _check64(tag, "multiple order 2", ms2[idx], ref)
+    dens3 = _flat(o3["scattering_density"]).astype(f64)
+    _check64(tag, "density order 3", dens3[idx],
+             oracle.scattering_density(p, 3, tr, None, None, ms2, e1, idx=idx, dtype=f64))
+    e2 = _flat(o3["delta_irradiance_0"]).astype(f64)
+    _check64(tag, "indirect order 2", e2, oracle.indirect_irradiance(p, 2, None, None, ms2, dtype=f64))
+    ms3 = _flat(o3["delta_multiple_scattering"]).astype(f64)
+    ref, _ = oracle.multiple_scattering(p, tr, dens3, idx=idx, dtype=f64)
+    _check64(tag, "multiple order 3", ms3[idx], ref)
+
+
+@pytest.mark.parametrize("i", HEADLINE)
+def test_headline_draw_each_pass_default_size(builder, oracle, i):
+    p = _draws()[i]
+    assert p.precision == PRECISION_MIXED
+    _passes_vs_fp64(builder, oracle, p, "headline draw %d, default size" % i)
+
+
+@pytest.mark.parametrize("i", HEADLINE)
+def test_headline_draw_end_to_end_dump_size(builder, oracle, i):
+    q = dump_parameters()
+    p = _draws()[i].replace(scattering_r_size=q.scattering_r_size, scattering_mu_size=q.scattering_mu_size,
+                            scattering_mu_s_size=q.scattering_mu_s_size, scattering_nu_size=q.scattering_nu_size)
+    assert p.order == 4 and p.precision == PRECISION_MIXED
+    out = _build(builder, p)
+    ref = oracle.precompute(p, np.float64)
+    for k in KEYS:
+        _check64("headline draw %d, dump size, order 4" % i, k, out[k], ref[k])
+
+
+@pytest.mark.parametrize("size", ["smoke", "dump"])
+@pytest.mark.parametrize("order", [5, 6, 7, 8])
+def test_high_orders_end_to_end(builder, oracle, size, order):
+    mk = smoke_parameters if size == "smoke" else dump_parameters
+    pm = mk(order=order, precision=PRECISION_MIXED)
+    out = _build(builder, pm)
+    ref = oracle.precompute(pm, np.float64)
+    for k in KEYS:
+        _check64("%s size, order %d, mixed" % (size, order), k, out[k], ref[k])
+    pp = mk(order=order)
+    out = _build(builder, pp)
+    ref = oracle.precompute(pp)
+    for k in KEYS:
+        assert np.isfinite(out[k]).all(), k
+        s = summary(out[k], ref[k])
+        _report("%s size, order %d, plain vs FP32" % (size, order), k, s)
+        assert s["max"] <= PLAIN_MAX and s["rms"] <= PLAIN_RMS, (k, s)
+
+
+def test_4x_resolution_order_8(builder, oracle):
+    """Order 8 at 4x resolution, MIXED: density of order 8 (reading the GPU's
+    order-7 multiple scattering and order-6 irradiance), indirect irradiance
+    of order 7 and multiple scattering of order 8 against FP64."""
+    f64 = np.float64
+    p = Parameters(precision=PRECISION_MIXED).replace(**workloads.CLASSES["double"])
+    b7 = _build(builder, p.replace(order=7), intermediates=True)
+    b8 = _build(builder, p.replace(order=8), intermediates=True)
+    ntr, nir, nsc = p.texel_counts()
+    rng = np.random.default_rng(8)
+    idx = np.sort(rng.choice(nsc, 4096, replace=False)).astype(np.int64)
+    tr = _flat(b8["transmittance"]).astype(f64)
+    ms7 = _flat(b7["delta_multiple_scattering"]).astype(f64)
+    e6 = _flat(b8["delta_irradiance_0"]).astype(f64)  # read by the order-8 density (order & 1 = 0)
+    dens8 = _flat(b8["scattering_density"]).astype(f64)
+    tag = "4x resolution"
+    _check64(tag, "density order 8", dens8[idx],
+             oracle.scattering_density(p.replace(order=8), 8, tr, None, None, ms7, e6, idx=idx, dtype=f64))
+    e7 = _flat(b8["delta_irradiance_1"]).astype(f64)
+    _check64(tag, "indirect order 7", e7, oracle.indirect_irradiance(p, 7, None, None, ms7, dtype=f64))
+    ms8 = _flat(b8["delta_multiple_scattering"]).astype(f64)
+    ref, _ = oracle.multiple_scattering(p, tr, dens8, idx=idx, dtype=f64)
+    _check64(tag, "multiple order 8", ms8[idx], ref)
+    # the order-7 build's last indirect irradiance is order 6: the same table
+    # the order-8 build's density read
+    assert np.array_equal(_flat(b7["delta_irradiance_0"]), _flat(b8["delta_irradiance_0"]))

@@ -71,3 +71,39 @@ def test_noalloc_refuses_builds_beyond_its_scratch(native_lib):
                                                 ctypes.c_void_p(buf.data_ptr()), ctypes.c_void_p(buf.data_ptr()))
     assert rc == N.FB_ERR_BUDGET
     assert b"scratch" in native_lib.fb_last_error()
+
+
+def test_noalloc_error_enqueues_nothing(native_lib):
+    """A build whose second pass cannot run (single scattering with 1024 steps
+    on rows of 16 texels needs more shared memory than a CTA can have) is
+    refused before anything is enqueued: the caller's tables keep their
+    contents, and the next call still builds correctly."""
+    import torch
+    from fuzzyblue_gb300 import _native as N
+    from fuzzyblue_gb300.api import Builder
+    torch.cuda.set_device(0)
+    p = smoke_parameters().replace(single_scattering_steps=1024)
+    tw, th = p.transmittance_extent()
+    iw, ih = p.irradiance_extent()
+    sw, sh, sd = p.scattering_extent()
+    sentinel = 1234.5
+    tr = torch.full((th, tw, 4), sentinel, dtype=torch.float32, device="cuda")
+    ir = torch.full((ih, iw, 4), sentinel, dtype=torch.float32, device="cuda")
+    sc = torch.full((sd, sh, sw, 4), sentinel, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    c = p.to_c()
+    rc = native_lib.fb_atmosphere_build_noalloc(ctypes.c_void_p(stream.cuda_stream), ctypes.byref(c),
+                                                ctypes.c_void_p(tr.data_ptr()), ctypes.c_void_p(ir.data_ptr()),
+                                                ctypes.c_void_p(sc.data_ptr()))
+    assert rc == N.FB_ERR_INVALID_PARAMS, native_lib.fb_last_error()
+    assert b"shared memory" in native_lib.fb_last_error()
+    torch.cuda.synchronize()
+    for t in (tr, ir, sc):
+        assert bool((t == sentinel).all())
+    b = Builder(0)
+    q = smoke_parameters()
+    ref = _reference_tables(b, q)
+    got = _noalloc_tables(native_lib, q)
+    for k in ("transmittance", "irradiance", "scattering"):
+        assert np.array_equal(got[k], ref[k]), k
+    b.close()
