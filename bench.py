@@ -16,6 +16,10 @@ FP64 oracle), built with one persistent launch per pass group.
   cpu_baseline  the reference's own shader code compiled as C++ (oracle/_ref), or
           the oracle port where that is unavailable, on a bounded sample, all
           host threads
+  uneven  one step of the uneven batch (96 atmospheres, three table classes,
+          orders 2-8), batched against the plain path per class
+  serve   a 12 s Poisson sample at 50 req/s through the request loop: p50/p99
+          latency overall and per class beside the plain FIFO replay
 
 --impl reference times the reference's CPU implementation on the same metric.
 Multi-GPU: replicas only (each rank builds its own batch; no collective on the
@@ -38,6 +42,8 @@ BATCH = 256
 ORDERS = 4
 WORKLOAD = ("uniform batch: 256 seeded atmospheres (seed 0), default table sizes "
             "(TR 256x64, IR 64x16, SC r32 mu128 mu_s32 nu8), 4 orders, mixed precision")
+SERVE_SAMPLE_RATE = 50.0      # req/s of the serving sample in the headline line
+SERVE_SAMPLE_SECONDS = 12.0   # seconds of arrivals of that sample
 METRIC = "atmospheres/s, uniform batch of 256 at default table sizes, 4 orders, mixed precision (<=1e-3 rel err vs FP64)"
 
 
@@ -50,6 +56,8 @@ def parse():
     ap.add_argument("--batch", type=int, default=BATCH)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="headline only: leave out the short uneven-batch and serving measurements")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "plain"],
                     help="arithmetic of the batch (the headline is mixed)")
     ap.add_argument("--workload", default="uniform", choices=["uniform", "uneven", "serve", "render"],
@@ -157,24 +165,35 @@ FLOP_PER_TEXEL = {
     "multiple_scattering": 8332.2,
 }
 FLOP_PER_ATMOSPHERE = 350185724984.0  # default sizes, 4 orders (same count)
-# committed ncu summaries the roofline figures come from
-DENSITY_PROFILE = "density_multiple_uniform16_mixed_ncu.md"
-LAUNCH_PROFILE = "launches_uniform256_mixed.md"
+# Counts of the dominant launch measured with ncu on the kernel sources whose
+# SHA-256 (first 16 hex digits, over KERNEL_SOURCES) is `sources`: the
+# executed FP32 FLOPs and thread instructions per direction evaluation (a
+# --set full capture of 16 atmospheres) and the DRAM bytes per launch (the same
+# capture, scaled to the launch's atmospheres). The commands are in the profile
+# summaries named by `profile`. When the sources on disk differ, the roofline
+# is reported with "stale": true.
+KERNEL_SOURCES = ("fuzzyblue_gb300/csrc/fb_passes.cuh", "fuzzyblue_gb300/csrc/fb_device.cuh")
+DENSITY_NCU = {
+    "sources": "PENDING",
+    "profile": "profiles/density_multiple_uniform16_mixed_ncu.md",
+    "atmospheres": 16,
+    "fp32_flop_per_direction_order3": 25.18,
+    "thread_instr_per_direction_order3": 22.36,
+    "dram_bytes_per_atmosphere_order3": 4.33e9 / 256,
+}
+
+
+def kernel_sources_sha():
+    import hashlib
+    h = hashlib.sha256()
+    for f in KERNEL_SOURCES:
+        with open(os.path.join(ROOT, f), "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()[:16]
 
 
 def fp32_peak_tflops(sms, mhz):
     return sms * 128 * 2 * mhz * 1e6 / 1e12
-
-
-def profile_value(name, key):
-    """A `key: value` line of a committed ncu summary under profiles/."""
-    try:
-        for line in open(os.path.join(ROOT, "profiles", name)):
-            if line.startswith(key + ":"):
-                return float(line.split(":", 1)[1])
-    except (OSError, ValueError):
-        pass
-    return None
 
 
 def measured_peaks():
@@ -341,26 +360,27 @@ def run_ours(a):
     # executed FP32 FLOPs per direction evaluation of this launch (ncu) and
     # the reference's quadrature FLOPs per texel (oracle op count)
     directions = a.batch * sizes[2] * 2 * params[0].density_samples ** 2
-    exec_per_dir = profile_value(DENSITY_PROFILE, "fp32_flop_per_direction_order3")
+    exec_per_dir = DENSITY_NCU["fp32_flop_per_direction_order3"]
+    stale = kernel_sources_sha() != DENSITY_NCU["sources"]
     ref_flops = a.batch * (sizes[2] * FLOP_PER_TEXEL["density_order3"] + sizes[1] * FLOP_PER_TEXEL["indirect_order2"])
     mhz = (clk or {}).get("sm_mhz") or 2070.0
     peak = fp32_peak_tflops(sms, mhz)
     exec_flops = directions * exec_per_dir if exec_per_dir else None
     achieved = exec_flops / (dens_ms / 1e3) / 1e12 if exec_flops else None
     ref_achieved = ref_flops / (dens_ms / 1e3) / 1e12
-    traffic = profile_value(LAUNCH_PROFILE, "dram_bytes_per_launch_order3")
+    traffic = DENSITY_NCU["dram_bytes_per_atmosphere_order3"] * a.batch
     peaks = measured_peaks()
     # the launch's binding limit is instruction issue: warp instructions per
     # launch (ncu's thread instructions per direction / 32) against one per
     # cycle per scheduler, 4 schedulers per SM
-    instr_per_dir = profile_value(DENSITY_PROFILE, "thread_instr_per_direction_order3")
+    instr_per_dir = DENSITY_NCU["thread_instr_per_direction_order3"]
     issue = None
     if instr_per_dir:
         issue_achieved = directions * instr_per_dir / 32.0 / (dens_ms / 1e3) / 1e9
         issue_peak = sms * 4 * mhz * 1e6 / 1e9
         issue = {"achieved": issue_achieved, "peak": issue_peak, "unit": "G warp instructions/s",
                  "frac": issue_achieved / issue_peak, "thread_instr_per_unit": instr_per_dir,
-                 "source": "thread instructions per direction, ncu, profiles/" + DENSITY_PROFILE}
+                 "source": "thread instructions per direction, ncu, " + DENSITY_NCU["profile"]}
 
     out = {
         "metric": METRIC if a.precision == "mixed" else METRIC.replace(
@@ -393,9 +413,13 @@ def run_ours(a):
                                     "no tensor-core work, HBM far from its limit" % mhz,
                      "launch_ms": dens_ms, "flop_per_unit": exec_per_dir, "units_per_launch": directions,
                      "unit_name": "direction evaluations (texels x 512 sphere directions)",
-                     "flop_source": "executed FP32 FLOPs (FADD + FMUL + 2 FFMA) per direction, ncu, profiles/"
-                                    + DENSITY_PROFILE,
-                     "traffic": traffic, "traffic_source": "ncu DRAM bytes of the same launch, profiles/" + LAUNCH_PROFILE,
+                     "flop_source": "executed FP32 FLOPs (FADD + FMUL + 2 FFMA) per direction, ncu, "
+                                    + DENSITY_NCU["profile"],
+                     "traffic": traffic,
+                     "traffic_source": "ncu DRAM bytes of the same launch on %d atmospheres (%s), scaled to %d"
+                                       % (DENSITY_NCU["atmospheres"], DENSITY_NCU["profile"], a.batch),
+                     "stale": stale, "kernel_sources_sha256_16": kernel_sources_sha(),
+                     "counts_measured_on_sha256_16": DENSITY_NCU["sources"],
                      "hbm": {"achieved_gbs": traffic / (dens_ms / 1e3) / 1e9 if traffic else None,
                              "peak_gbs": peaks.get("hbm_gbs"), "peak_source": "MEASURED_PEAKS.json"},
                      "issue": issue,
@@ -413,6 +437,20 @@ def run_ours(a):
         "algorithmic_tflops": value * FLOP_PER_ATMOSPHERE / 1e12,
         "tile_shape": tuned,
     }
+    if rank == 0 and world == 1 and not a.no_extras:
+        # the other configurations in short form: one step of the uneven batch
+        # and a Poisson sample at 50 req/s through the request loop
+        u = measure_uneven(a, builder, stream, steps=1, warmup=1)
+        out["uneven"] = {k: u[k] for k in ("metric", "value", "unit", "ms_per_step", "e2e", "plain",
+                                           "batched_over_plain", "per_class", "clocks")}
+        out["uneven"]["steps"], out["uneven"]["warmup"] = 1, 1
+        sv = measure_serve(a, builder, [SERVE_SAMPLE_RATE], SERVE_SAMPLE_SECONDS)
+        line = sv["rates"][0]
+        out["serve"] = {"metric": sv["metric"], "offered_rate": line["offered_rate"],
+                        "duration_s": SERVE_SAMPLE_SECONDS, "requests": line["requests"],
+                        "served": line["served"], "plain_fifo": line["plain"],
+                        "served_over_plain_throughput": line["served_over_plain_throughput"],
+                        "config": sv["config"]}
     if rank == 0 and not a.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(params[0])
     if rank == 0:
@@ -603,15 +641,23 @@ def run_uneven(a):
     table classes, orders uniform in 2-8, one batch build per step (one
     persistent launch per pass group, replayed from a CUDA graph)."""
     world, rank, local = dist()
-    import numpy as np
     import torch
     torch.cuda.set_device(local)
-    from fuzzyblue_gb300 import workloads
-    from fuzzyblue_gb300.api import Builder, build_batch
-    from fuzzyblue_gb300.params import PRECISION_MIXED, PRECISION_PLAIN
-    from fuzzyblue_gb300 import _native as N
+    from fuzzyblue_gb300.api import Builder
     builder = Builder(local)
     stream = torch.cuda.Stream()
+    print(json.dumps(measure_uneven(a, builder, stream, a.steps, a.warmup)))
+    builder.close()
+
+
+def measure_uneven(a, builder, stream, steps, warmup):
+    """The uneven batch's line: device-resident rate, end to end, and batched
+    against the plain path overall and per table class."""
+    import torch
+    from fuzzyblue_gb300 import workloads
+    from fuzzyblue_gb300.api import build_batch
+    from fuzzyblue_gb300.params import PRECISION_MIXED, PRECISION_PLAIN
+    from fuzzyblue_gb300 import _native as N
     prec = PRECISION_MIXED if a.precision == "mixed" else PRECISION_PLAIN
     params = workloads.uneven_batch(96, seed=1, precision=prec)
     classes, seen = [], set()
@@ -623,23 +669,23 @@ def run_uneven(a):
     if not a.no_autotune:
         builder.autotune(classes, batch=4)
     tuned = [builder.tuned_shape(c) for c in classes]
-    for _ in range(a.warmup):
+    for _ in range(warmup):
         q = build_batch(builder, params, stream=stream)
         q.wait()
         q.release()
     torch.cuda.synchronize()
-    clocks = Clocks(local)
+    clocks = Clocks(torch.cuda.current_device())
     clocks.start()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for _ in range(a.steps):
+    for _ in range(steps):
         q = build_batch(builder, params, stream=stream)
         q.wait()
         q.release()
     e1.record(stream)
     torch.cuda.synchronize()
     clk = clocks.stop()
-    ms = e0.elapsed_time(e1) / a.steps
+    ms = e0.elapsed_time(e1) / steps
     # end to end: every table of every atmosphere into pinned host memory
     bufs = {}
     for p in params:
@@ -649,7 +695,7 @@ def run_uneven(a):
             bufs[key] = torch.empty(n, dtype=torch.float32, pin_memory=True).numpy()
     d2h = 0
     t0 = time.perf_counter()
-    for _ in range(a.steps):
+    for _ in range(steps):
         q = build_batch(builder, params, stream=stream)
         q.wait()
         for i, p in enumerate(params):
@@ -660,7 +706,7 @@ def run_uneven(a):
             d2h += 16 * (ntr + nir + nsc)
         q.release()
     torch.cuda.synchronize()
-    e2e_s = (time.perf_counter() - t0) / a.steps
+    e2e_s = (time.perf_counter() - t0) / steps
     per_class = {}
     for p in params:
         c = "x".join(str(v) for v in p.scattering_extent())
@@ -696,7 +742,7 @@ def run_uneven(a):
     out = {
         "metric": "atmospheres/s, uneven batch of 96 over three table classes, orders 2-8, %s precision"
                   % a.precision,
-        "value": 96 / (ms / 1e3), "unit": "atmospheres/s", "n_gpus": 1, "steps": a.steps, "warmup": a.warmup,
+        "value": 96 / (ms / 1e3), "unit": "atmospheres/s", "n_gpus": 1, "steps": steps, "warmup": warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 with f64 ray geometry and order accumulation" if a.precision == "mixed" else "f32",
         "data": "synthetic: seeded atmospheres (fuzzyblue_gb300.workloads.uneven_batch, seed 1)",
@@ -706,15 +752,14 @@ def run_uneven(a):
                    "l2": "inputs larger than L2"},
         "clocks": clk,
         "e2e": {"value": 96 / e2e_s, "unit": "atmospheres/s", "h2d_bytes_per_step": 96 * 384,
-                "d2h_bytes_per_step": d2h // a.steps},
+                "d2h_bytes_per_step": d2h // steps},
         "tile_shapes": tuned,
         "plain": {"atmospheres_per_s": 96 / plain_total, "precision": "plain",
                   "path": "each atmosphere alone, one call each, FP32"},
         "batched_over_plain": (96 / (ms / 1e3)) / (96 / plain_total),
         "per_class": compare,
     }
-    print(json.dumps(out))
-    builder.close()
+    return out
 
 
 # ---------------------------------------------------------------- serving ---
@@ -733,15 +778,23 @@ def run_serve(a):
     plain one-at-a-time path is measured as per-request build times of plain
     FP32 single builds per (class, order), replayed in arrival order through
     one FIFO server with the same queue limit."""
-    import threading
-    import numpy as np
     import torch
     torch.cuda.set_device(0)
+    from fuzzyblue_gb300.api import Builder
+    builder = Builder(0)
+    print(json.dumps(measure_serve(a, builder, [float(x) for x in a.rates.split(",")], a.duration)))
+    builder.close()
+
+
+def measure_serve(a, builder, rates, duration):
+    """The serving line: per offered rate, served throughput and latency
+    percentiles (overall and per class) beside the plain FIFO replay."""
+    import threading
+    import numpy as np
     from fuzzyblue_gb300 import workloads
     from fuzzyblue_gb300 import _native as N
-    from fuzzyblue_gb300.api import Atmosphere, Builder, Server
+    from fuzzyblue_gb300.api import Atmosphere, Server
     from fuzzyblue_gb300.params import PRECISION_MIXED, PRECISION_PLAIN
-    builder = Builder(0)
     names = ("default", "half", "double")
     prec = PRECISION_MIXED if a.precision == "mixed" else PRECISION_PLAIN
     probe = workloads.draw_atmosphere(np.random.default_rng(99), precision=prec)
@@ -768,12 +821,12 @@ def run_serve(a):
                 q.release()
             service[(c, order)] = min(ts[1:])
     lines = []
-    for rate in [float(x) for x in a.rates.split(",")]:
+    for rate in rates:
         rng = np.random.default_rng(2)
         arrivals, t = [], 0.0
         while True:
             t += float(rng.exponential(1.0 / rate))
-            if t > a.duration:
+            if t > duration:
                 break
             arrivals.append(t)
         reqs = [workloads.serving_request(rng, precision=prec) for _ in arrivals]
@@ -801,7 +854,7 @@ def run_serve(a):
         # finished tickets come from the server's completion queue
         # (fb_server_completed): one call per wake-up, not a poll per ticket
         failed = [0]
-        deadline = start + a.duration + 120.0
+        deadline = start + duration + 120.0
         while time.perf_counter() < deadline:
             for tk in srv.completed(timeout_ms=1):
                 now = time.perf_counter()
@@ -859,12 +912,11 @@ def run_serve(a):
         "data": "synthetic: seeded requests (fuzzyblue_gb300.workloads.serving_request, seed 2)",
         "config": {"workload": "serving: open-loop Poisson requests, class 60/30/10 default / half / double, "
                                "orders 2-8, 120 GB HBM budget, LRU-resident tables",
-                   "duration_s": a.duration, "max_queue": a.max_queue, "precision": a.precision,
+                   "duration_s": duration, "max_queue": a.max_queue, "precision": a.precision,
                    "plain_path": "plain FP32 single builds per (class, order), measured, replayed FIFO"},
         "rates": lines,
     }
-    print(json.dumps(out))
-    builder.close()
+    return out
 
 
 def main():

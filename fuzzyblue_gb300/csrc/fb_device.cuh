@@ -515,6 +515,25 @@ struct Geo64 {
 // every later step in FP32 on quantities that no longer cancel. Same results
 // as Geo64 to FP32 precision, at a fraction of its FP64 instructions (FP64
 // issues at 1/64 of the FP32 rate on this part).
+// An axis of a table measured from its last texel: g >= 0 texels before
+// texel n - 1, i.e. at texel coordinate n - 1 - g. The interpolation runs from
+// the edge texel (i0) towards the inner one (i1) with weight f = frac(g), so
+// that near the edge the position keeps the relative precision of g; an FP32
+// coordinate near n - 1 itself has a resolution of ulp(n - 1) (1.5e-5 texels
+// at n = 256). NaN maps to the edge texel.
+__device__ __forceinline__ Axis edge_axis(float g, int n) {
+  float k = floorf(g);
+  Axis a;
+  a.f = g - k;
+  k = fminf(fmaxf(k, 0.0f), float(n));  // fmaxf(NaN, 0) = 0
+  const int i = (int)k;
+  a.i0 = max(n - 1 - i, 0);
+  a.i1 = max(n - 2 - i, 0);
+  return a;
+}
+
+// Geometry of the mixed mode's per-sample records: FP64 ray state (q = r^2 -
+// R^2, s = r mu), the rest in FP32.
 struct GeoMx {
   float R, T, H, H2f, inv_H, trm1, trr1, scr1, M1f, Mf;
   double H2;
@@ -539,19 +558,31 @@ struct GeoMx {
     e_out = ef;
     return fmaxf(sf > 0.0f ? __fdividef(ef, sf + root) : root - sf, 0.0f);
   }
-  __device__ __forceinline__ void tr_texel(double q, double s, float& tx, float& ty) const {
+  // transmittance.h:7-24 as axes of the transmittance table, the mu axis
+  // measured from its horizon edge. Along rays near the horizon the table
+  // changes by large factors per texel (e^7 between the last two texels for
+  // some atmospheres), so the texel position there must keep more than FP32's
+  // absolute resolution near texel N - 1. With delta = s^2 - q (FP64), the gap
+  // d_max - d between the horizon distance rho + H and the distance to the top
+  // d = -s + sqrt(H^2 + delta) is (rho + s) + (H - sqrt(H^2 + delta)), each
+  // part formed without cancellation: rho + s = -delta / (rho - s) for s < 0,
+  // H - sqrt(H^2 + delta) = -delta / (H + sqrt(H^2 + delta)). The texel
+  // position is N - 1 - g with g = (N - 1) gap / (d_max - d_min).
+  __device__ __forceinline__ void tr_axes(double q, double s, int tr_mu, int tr_r, Axis& ax, Axis& ay) const {
     const float qf = fmaxf((float)q, 0.0f);
     const float rho = sqrtf(qf), r = sqrtf(qf + R * R);
-    float e;
-    const float d = dist_top(q, s, e);
-    const float d_min = __fdividef(e, T + r);
-    tx = __fdividef(d - d_min, rho + H - d_min) * trm1;
-    ty = rho * inv_H * trr1;
+    const float delta = (float)fma(s, s, -q), sf = (float)s;
+    const float root = sqrtf(fmaxf(H2f + delta, 0.0f));
+    const float rho_s = sf < 0.0f ? -delta / (rho - sf) : rho + sf;
+    const float gap = fmaxf(rho_s - delta / (H + root), 0.0f);
+    const float d_min = (float)(H2 - q) / (T + r);
+    ax = edge_axis(gap / (rho + H - d_min) * trm1, tr_mu);
+    ay = axis_texel(rho * inv_H * trr1, tr_r);
   }
   __device__ __forceinline__ float3 tr_to_top(const DevAtmo& a, double q, double s) const {
-    float tx, ty;
-    tr_texel(q, s, tx, ty);
-    return fetch2(a.tr, a.tr_mu, axis_texel(tx, a.tr_mu), axis_texel(ty, a.tr_r));
+    Axis ax, ay;
+    tr_axes(q, s, a.tr_mu, a.tr_r, ax, ay);
+    return fetch2(a.tr, a.tr_mu, ax, ay);
   }
   __device__ __forceinline__ float3 tr_segment(const DevAtmo& a, double q, double s, double d, bool ground) const {
     double qd = fma(d, 2.0 * s + d, q), sd = s + d;

@@ -847,9 +847,8 @@ struct DensLayout {
   DensTheta* th;    // NT
   Axis* tay;        // NT: theta -> mu axis
   Axis* kax;        // S * NK: (column, nu slice) -> x axis
-  float4* dir;      // NT * NT mirror pairs: (cos phi sin t, sin phi sin t) x (nu_size - 1) / 2,
-                    // (ground normal x, y) x (ir_mus - 1) / 2
-  float* gnz;       // NT * NT: ground normal z x (ir_mus - 1) / 2
+  float2* dir;      // NT * NT mirror pairs: (cos phi sin t, sin phi sin t) x (nu_size - 1) / 2
+  float2* gw;       // NT: ground rows, the ground table position as a function of w: (A, B0)
   LerpRec* P;       // S * NT * MK: nu intervals of the previous order (dens_mk); order 2:
                     // LerpRec2 records of the Rayleigh and Mie tables
   LerpRec* E;       // MKE: intervals of the ground irradiance row, the two sampler rows pre-blended (dens_mke)
@@ -871,7 +870,7 @@ __host__ __device__ inline size_t dens_layout(unsigned char* base, int dens_n, i
     return at;
   };
   size_t o_th = take(sizeof(DensTheta) * NT), o_tay = take(sizeof(Axis) * NT), o_kax = take(sizeof(Axis) * S * NK);
-  size_t o_dir = take(sizeof(float4) * NT * NT), o_gnz = take(sizeof(float) * NT * NT);
+  size_t o_dir = take(sizeof(float2) * NT * NT), o_gw = take(sizeof(float2) * NT);
   size_t o_P = take((two ? sizeof(LerpRec2) : sizeof(LerpRec)) * nP), o_E = take(sizeof(LerpRec) * dens_mke(ir_mus, cl));
   size_t o_cm = take(sizeof(float) * S), o_cmd = take(sizeof(double) * S);
   size_t o_ymu = take(mixed ? sizeof(double2) * chunk : 0), o_nu = take(mixed ? sizeof(double) * sc_nu : 0);
@@ -880,8 +879,8 @@ __host__ __device__ inline size_t dens_layout(unsigned char* base, int dens_n, i
     L->th = (DensTheta*)(base + o_th);
     L->tay = (Axis*)(base + o_tay);
     L->kax = (Axis*)(base + o_kax);
-    L->dir = (float4*)(base + o_dir);
-    L->gnz = (float*)(base + o_gnz);
+    L->dir = (float2*)(base + o_dir);
+    L->gw = (float2*)(base + o_gw);
     L->P = (LerpRec*)(base + o_P);
     L->E = (LerpRec*)(base + o_E);
     L->col_mus = (float*)(base + o_cm);
@@ -932,11 +931,18 @@ template <bool CL> __device__ __forceinline__ int line_pos(float w, int n) {
 // bounce (scattering_density.comp:64-84), times the phase functions
 // (scattering_density.comp:86-104). Table positions come as w = t - 1/2
 // (line_pos): the direction table holds cos phi sin t and sin phi sin t scaled
-// by (nu_size - 1) / 2 and the ground normal scaled by (ir_mus - 1) / 2, and
-// the row and column terms carry the offsets.
+// by (nu_size - 1) / 2, and the row and column terms carry the offsets.
+//
+// The ground bounce's lookup position is an affine function of the nu table's
+// position w on a theta row: where omega_i meets the ground, at distance dg,
+// the normal is n = (r zenith + dg omega_i) / R (the hit point lies on the
+// sphere of radius R), so n . omega_s = (dg / R) nu_i + (r / R) mu_s with
+// nu_i = omega_i . omega_s = (w + 1/2) / hP - 1. The position in the ground
+// irradiance table, we = hE (n . omega_s + 1) - 1/2, is then A w + B with A =
+// hE dg / (R hP) per row and B = B0 + hE (r / R) mu_s per row and texel column.
 struct DensRowConst {
   float mu, muh, mu_s, oxs;  // mu; mu_s (nu_size - 1) / 2; mu_s; sqrt(1 - mu^2) / ((nu_size - 1) / 2)
-  float offP, offE;          // (n - 1) / 2 - 1/2 of the nu and ground irradiance tables
+  float offP, gmus;          // (n - 1) / 2 - 1/2 of the nu table; hE (r / R) mu_s
   float inv_h, c1;           // TWO: nu = w inv_h + c1
   int nP, nE;                 // records per nu table row and of the ground irradiance table
 };
@@ -947,19 +953,22 @@ __device__ __forceinline__ void dens_row(const DensLayout& S, const DensTheta& t
                                          const float (&sy)[kDensMaxGroup], int G, const PhaseCoef& pc,
                                          float3 (&acc)[kDensMaxGroup]) {
   const float mus_ct = fmaf(q.muh, t.cos_t, q.offP), mu_ct = q.mu * t.cos_t;
-  const float4* dirl = S.dir + l * NT;
-  const float* gnzl = S.gnz + l * NT;
+  const float2* dirl = S.dir + l * NT;
+  float gA = 0.f, gB = 0.f;
+  if (GROUND) {
+    const float2 g = S.gw[l];
+    gA = g.x;
+    gB = g.y + q.gmus;
+  }
   for (int m = 0; m < NT; ++m) {
-    const float4 d = dirl[m];
+    const float2 d = dirl[m];
     // phase functions of omega . omega_i, shared by the pair and the group
     const float nu2 = fmaf(q.oxs, d.x, mu_ct);
     const float3 cf = pc.eval(nu2, t.domega);
-    const float gzm = GROUND ? fmaf(gnzl[m], q.mu_s, q.offE) : 0.f;
 #pragma unroll
     for (int j = 0; j < kDensMaxGroup; ++j) {
       if (j < G) {
         const float base = fmaf(sx[j], d.x, mus_ct), dy = sy[j] * d.y;
-        const float gb = GROUND ? fmaf(d.z, sx[j], gzm) : 0.f, gdy = GROUND ? d.w * sy[j] : 0.f;
 #pragma unroll
         for (int side = 0; side < 2; ++side) {
           const float w = side ? base - dy : base + dy;
@@ -984,7 +993,7 @@ __device__ __forceinline__ void dens_row(const DensLayout& S, const DensTheta& t
           }
           if (GROUND) {
             // irradiance of order n - 2 where omega_i meets the ground
-            const float we = side ? gb - gdy : gb + gdy;
+            const float we = fmaf(gA, w, gB);
             const int e = line_pos<CL>(we, q.nE);
             const float4 ea = S.E[e].a;
             const float2 eb = S.E[e].b;
@@ -1099,13 +1108,12 @@ __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned cha
       const int l = k / NT, m = k % NT;
       const float st = sinf((float(l) + 0.5f) * dtheta);
       const float phi = (float(m) + 0.5f) * dphi;
-      const float cx = cosf(phi) * st, cy = sinf(phi) * st;
-      // normalize(zenith * r + omega_i * distance_to_ground)
-      const float dg = S.th[l].dg, ct = S.th[l].cos_t;
-      const float gx = cx * dg, gy = cy * dg, gz = r + ct * dg;
-      const float len = sqrtf(gx * gx + gy * gy + gz * gz);
-      S.dir[k] = make_float4(cx * hP, cy * hP, gx / len * hE, gy / len * hE);
-      S.gnz[k] = gz / len * hE;
+      S.dir[k] = make_float2(cosf(phi) * st * hP, sinf(phi) * st * hP);
+    }
+    // ground rows: the ground table position we = A w + B0 + hE (r / R) mu_s
+    for (int l = tid; l < NT; l += nth) {
+      const float g = S.th[l].dg / a.bottom;
+      S.gw[l] = make_float2(hE * g / hP, fmaf(hE, fmaf(g, 0.5f / hP - 1.0f, 1.0f), -0.5f));
     }
     // interval ki (entries ki, ki + 1) for ki < ir_mus; interval -1 (below
     // entry 0) holds entry 0's value
@@ -1251,7 +1259,7 @@ __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned cha
     q.mu_s = mu_s;
     q.oxs = ox / hP;
     q.offP = hP - 0.5f;
-    q.offE = hE - 0.5f;
+    q.gmus = hE * (r / a.bottom) * mu_s;
     q.inv_h = 1.0f / hP;
     q.c1 = 0.5f / hP - 1.0f;
     q.nP = MK;

@@ -5,10 +5,11 @@
    with the smallest planet (index 95, bottom radius 3001 km), the thinnest
    atmosphere (index 216, 40.7 km) and the largest Mie coefficient (index 161).
    At the default table sizes in MIXED precision, every pass of the GPU against
-   the FP64 oracle's same pass on the GPU's own inputs (sampled texels, as in
-   test_parity_gpu.test_each_pass_at_default_size); at the sizes of the crate's
-   dump example (r16 mu64 mu_s16 nu4, 4 orders) the whole precompute against
-   the FP64 oracle on every texel.
+   the FP64 oracle's same pass on the GPU's own inputs (random texels, as in
+   test_parity_gpu.test_each_pass_at_default_size, plus the rows of rays at the
+   horizon, where the transmittance table changes by large factors per texel);
+   at the sizes of the crate's dump example (r16 mu64 mu_s16 nu4, 4 orders) the
+   whole precompute against the FP64 oracle on every texel.
 2. Orders 5-8 (the uneven and serving workloads draw orders in 2-8; the
    reference's order loop, src/precompute.rs:1853-1999, accumulates every
    order into the scattering and irradiance tables,
@@ -73,11 +74,27 @@ def _flat(a):
     return np.ascontiguousarray(a.reshape(-1, 4))
 
 
+def _horizon_rows(p):
+    """Every texel of the scattering rows whose rays graze the horizon: mu
+    rows 0 and M - 1 (ground half) and M and 2M - 1 (sky half, row 2M - 1 the
+    ray tangent to the ground), at every r."""
+    sw, sh, sd = p.scattering_extent()
+    M = sh // 2
+    rows = [(z, y) for z in range(sd) for y in (0, M - 1, M, 2 * M - 1)]
+    return np.concatenate([np.arange(sw) + (z * sh + y) * sw for z, y in rows]).astype(np.int64)
+
+
+def _sampled(rng, n, k, extra):
+    return np.unique(np.concatenate([rng.choice(n, k, replace=False).astype(np.int64), extra]))
+
+
 def _passes_vs_fp64(builder, oracle, p, tag, samples=512):
-    """Orders 2 and 3 of a MIXED build: every pass against the FP64 oracle."""
+    """Orders 2 and 3 of a MIXED build: every pass against the FP64 oracle, on
+    random texels plus every texel of the horizon rows."""
     f64 = np.float64
     rng = np.random.default_rng(11)
     ntr, nir, nsc = p.texel_counts()
+    hz = _horizon_rows(p)
     o2 = _build(builder, p.replace(order=2), intermediates=True)
     o3 = _build(builder, p.replace(order=3), intermediates=True)
     tr = _flat(o2["transmittance"]).astype(f64)
@@ -86,11 +103,11 @@ def _passes_vs_fp64(builder, oracle, p, tag, samples=512):
     d0 = _flat(o2["delta_irradiance_0"]).astype(f64)
     _check64(tag, "direct irradiance", d0, oracle.direct_irradiance(p, tr, dtype=f64))
     dr, dm = _flat(o2["delta_rayleigh"]).astype(f64), _flat(o2["delta_mie"]).astype(f64)
-    idx = np.sort(rng.choice(nsc, samples * 2, replace=False)).astype(np.int64)
+    idx = _sampled(rng, nsc, samples * 2, hz)
     r, m = oracle.single_scattering(p, tr, idx=idx, dtype=f64)
     _check64(tag, "single rayleigh", dr[idx], r)
     _check64(tag, "single mie", dm[idx], m)
-    idx = np.sort(rng.choice(nsc, samples, replace=False)).astype(np.int64)
+    idx = _sampled(rng, nsc, samples, hz[::8])
     dens2 = _flat(o2["scattering_density"]).astype(f64)
     _check64(tag, "density order 2", dens2[idx],
              oracle.scattering_density(p, 2, tr, dr, dm, None, d0, idx=idx, dtype=f64))
