@@ -274,7 +274,9 @@ void fb_atmosphere_destroy(fb_atmosphere* a);
  * enqueued on `stream` for the current device. All calls share that array
  * and it keeps the last call's contents: calls whose GPU work overlaps race on
  * it, so serialise them. The first call on a device sets the device up; make
- * it before any stream capture. */
+ * it before any stream capture. Every check runs before anything is enqueued:
+ * a call that returns an error has enqueued nothing and left the tables
+ * untouched. */
 int fb_atmosphere_build_noalloc(void* stream, const fb_params* p,
                                 void* transmittance, void* irradiance,
                                 void* scattering);
