@@ -148,6 +148,15 @@ __device__ __forceinline__ double gclamp(double x, double lo, double hi) { retur
 
 template <class T> __device__ __forceinline__ T clamp_cosine(T mu) { return gclamp(mu, T(-1), T(1)); }
 __device__ __forceinline__ float safe_sqrt(float a) { return sqrtf(gmax(a, 0.0f)); }
+// 1 / sqrt(x) for arguments that are positive and normal: the hardware
+// reciprocal square root alone (PTX rsqrt.approx.ftz.f32). rsqrtf adds a test
+// and a rescaling for subnormal arguments; for normal ones the result is the
+// same. Callers pass only arguments bounded away from zero.
+__device__ __forceinline__ float rsqrt_pos(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
 __device__ __forceinline__ double safe_sqrt(double a) { return sqrt(gmax(a, 0.0)); }
 
 // util.h:18-24
@@ -640,7 +649,7 @@ struct MuS32 {
   __device__ __forceinline__ float texel(float mu_s) const {
     float s = R * mu_s;
     const float disc = fmaf(s, s, H2);  // >= H^2 > 0
-    float root = disc * rsqrtf(disc);
+    float root = disc * rsqrt_pos(disc);  // disc >= H^2
     const bool up = s > 0.0f;
     const float P = up ? H2 : root - s, Q = up ? s + root : 1.0f;
     const float aQ = fmaf(-dmin, Q, P) * inv_span;

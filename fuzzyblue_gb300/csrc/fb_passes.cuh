@@ -693,7 +693,7 @@ __device__ void tile_single(const DevAtmo& a, int tile, unsigned char* smem) {
         // square root as x rsqrt(x) (a few ulp; 0 where the argument is 0,
         // on the top boundary)
         const float disc = fmaf(s_d, s_d, o.e);
-        const float root = disc > 0.0f ? disc * rsqrtf(disc) : 0.0f;
+        const float root = disc > 1e-30f ? disc * rsqrt_pos(disc) : 0.0f;
         float dt = s_d > 0.0f ? __fdividef(o.e, s_d + root) : root - s_d;
         x_mu = (dt - o.dmin) * o.inv_span;
       }
@@ -900,7 +900,7 @@ struct PhaseCoef {
   float g1, g2;
   __device__ __forceinline__ float3 eval(float nu, float scale) const {
     const float t1 = fmaf(nu, nu, 1.0f) * scale;
-    const float rs = rsqrtf(fmaf(-g2, nu, g1));
+    const float rs = rsqrt_pos(fmaf(-g2, nu, g1));
     const float rs3 = rs * rs * rs;
     return make_float3(fmaf(B.x, rs3, A.x) * t1, fmaf(B.y, rs3, A.y) * t1, fmaf(B.z, rs3, A.z) * t1);
   }
@@ -985,7 +985,7 @@ __device__ __forceinline__ void dens_row(const DensLayout& S, const DensTheta& t
             const float4 ra = r2.a, rb = r2.b, rc = r2.c;
             const float nu1 = fmaf(w, q.inv_h, q.c1);
             const float t1 = fmaf(nu1, nu1, 1.0f);
-            const float rs = rsqrtf(fmaf(-pc.g2, nu1, pc.g1));
+            const float rs = rsqrt_pos(fmaf(-pc.g2, nu1, pc.g1));
             const float rs3 = rs * rs * rs;
             inc.x = fmaf(fmaf(rc.y, w, rb.z), rs3, fmaf(ra.w, w, ra.x)) * t1;
             inc.y = fmaf(fmaf(rc.z, w, rb.w), rs3, fmaf(rb.x, w, ra.y)) * t1;
@@ -1315,12 +1315,33 @@ __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned cha
 }
 
 // ================================================== indirect irradiance ===
-// indirect_irradiance.comp:10-74. One CTA per irradiance texel: the CTA
-// reduces the order's table to P[theta][nu slice] at its (r, mu_s), threads
-// split the 16 x 64 directions, and warp shuffles plus one shared-memory step
-// sum them.
+// indirect_irradiance.comp:10-74. A work item is K irradiance texels (K = 4
+// where shared memory allows, see ir_per_item), one warp per texel: the warp
+// reduces the order's table to P[theta][nu slice] at its texel's (r, mu_s),
+// its lanes split the 16 x 64 directions, and a warp shuffle sums them. The
+// CTA first tabulates the directions once for its K texels: per direction
+// cos phi sin theta, per theta row cos theta and the solid angle (the same
+// float arithmetic as evaluating them per direction).
+constexpr int kIrMaxPerItem = 4;  // texels per item: one per warp of a kDensThreads CTA
+constexpr size_t kIrItemSmem = 64 * 1024;
+__host__ __device__ inline size_t indirect_smem_k(int irr_n, int sc_nu, bool one, int k) {
+  const size_t NT = irr_n / 2, NP = 2 * (size_t)irr_n;
+  return align16(sizeof(float) * NT * NP) + align16(sizeof(float2) * NT) +
+         (size_t)k * sizeof(float4) * NT * (sc_nu + 2) * (one ? 2 : 1);
+}
+// Texels per item: 4, 2 or 1, the most whose tables fit in kIrItemSmem (the
+// order-1 layout, the larger one, decides for every order).
+__host__ __device__ inline int ir_per_item(int irr_n, int sc_nu) {
+  int k = kIrMaxPerItem;
+  while (k > 1 && indirect_smem_k(irr_n, sc_nu, true, k) > kIrItemSmem) k >>= 1;
+  return k;
+}
 __host__ __device__ inline size_t indirect_smem(int irr_n, int sc_nu, bool one) {
-  return sizeof(float4) * (size_t)(irr_n / 2) * (sc_nu + 2) * (one ? 2 : 1) + sizeof(double) * 3 * 32;
+  return indirect_smem_k(irr_n, sc_nu, one, ir_per_item(irr_n, sc_nu));
+}
+__host__ __device__ inline int tiles_indirect(int ir_mus, int ir_r, int irr_n, int sc_nu) {
+  const int k = ir_per_item(irr_n, sc_nu);
+  return (ir_mus * ir_r + k - 1) / k;
 }
 
 template <bool MX>
@@ -1329,52 +1350,67 @@ __device__ void tile_indirect(const DevAtmo& a, int order, int tile, unsigned ch
   const bool one = ord == 1;
   const int NT = a.irr_n / 2, NP = 2 * a.irr_n;
   const int NNU = a.sc_nu, NK = NNU + 2;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  float4* P = (float4*)smem;
-  double* red = (double*)(P + (size_t)NT * NK * (one ? 2 : 1));
-  const int t = tile;
-  const int i = t % a.ir_mus, j = t / a.ir_mus;
-  float r, mu_s, u_ms = 0.f;
-  Axis az;
-  if (!MX) {
-    Geo32 G;
-    G.init(a);
-    const float x_mu_s = float(i) / float(a.ir_mus - 1), x_r = float(j) / float(a.ir_r - 1);
-    r = G.R + x_r * (G.T - G.R);
-    mu_s = clamp_cosine(2.0f * x_mu_s - 1.0f);
-    az = make_axis(G.u_r(a, r), a.sc_r);
-    u_ms = G.u_mu_s(a, mu_s);
-  } else {
-    // the FP64 decodes come from the records of the build (tile_irgeo)
-    const IrZ z = a.g_irz[j];
-    r = z.r;
-    az = bounded_axis(z.az, a.sc_r);
-    mu_s = a.g_irmus[i];
-  }
-  const float4* src0 = one ? a.dr : a.dms;
+  const int K = ir_per_item(a.irr_n, a.sc_nu);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nth = blockDim.x;
+  float* Dcx = (float*)smem;                                          // NT * NP: cos phi sin theta
+  float2* Drow = (float2*)(smem + align16(sizeof(float) * NT * NP));  // NT: (cos theta, d omega)
+  float4* Pall = (float4*)((unsigned char*)Drow + align16(sizeof(float2) * NT));
   const float dthetaf = kPiF / float(a.irr_n), dphif = kPiF / float(a.irr_n);
-  const int nth = blockDim.x;
-  for (int k = tid; k < NT * NK; k += nth) {
-    const int l = k / NK, s = k % NK;
-    Axis ay, ax;
+  for (int k = tid; k < NT * NP; k += nth) {
+    const int l = k / NP, m = k % NP;
+    const float theta = (float(l) + 0.5f) * dthetaf, phi = (float(m) + 0.5f) * dphif;
+    Dcx[k] = cosf(phi) * sinf(theta);
+    if (m == 0) Drow[l] = make_float2(cosf(theta), dthetaf * dphif * sinf(theta));
+  }
+  const int t = tile * K + warp;
+  const bool active = warp < K && t < a.ir_mus * a.ir_r;
+  const int PS = NT * NK;  // entries of one table
+  float4* P = Pall + (size_t)(warp < K ? warp : 0) * PS * (one ? 2 : 1);
+  const int i = t % a.ir_mus, j = t / a.ir_mus;
+  float r = 0.f, mu_s = 0.f, u_ms = 0.f;
+  Axis az;
+  az.i0 = az.i1 = 0;
+  az.f = 0.f;
+  if (active) {
     if (!MX) {
       Geo32 G;
       G.init(a);
-      const float ct = cosf((float(l) + 0.5f) * dthetaf);
-      ay = make_axis(G.u_mu(a, r, ct, false), a.sc_mu);
-      ax = make_axis((float(s - 1) + u_ms) / float(NNU), a.W);
+      const float x_mu_s = float(i) / float(a.ir_mus - 1), x_r = float(j) / float(a.ir_r - 1);
+      r = G.R + x_r * (G.T - G.R);
+      mu_s = clamp_cosine(2.0f * x_mu_s - 1.0f);
+      az = make_axis(G.u_r(a, r), a.sc_r);
+      u_ms = G.u_mu_s(a, mu_s);
     } else {
-      ay = bounded_axis(a.g_iry[j * NT + l], a.sc_mu);
-      ax = bounded_axis(a.g_irx[i * NK + s], a.W);
+      // the FP64 decodes come from the records of the build (tile_irgeo)
+      const IrZ z = a.g_irz[j];
+      r = z.r;
+      az = bounded_axis(z.az, a.sc_r);
+      mu_s = a.g_irmus[i];
     }
-    const float3 v = fetch3(src0, a.W, a.sc_mu, ax, ay, az);
-    P[k] = make_float4(v.x, v.y, v.z, 0.f);
-    if (one) {
-      const float3 m = fetch3(a.dm, a.W, a.sc_mu, ax, ay, az);
-      P[NT * NK + k] = make_float4(m.x, m.y, m.z, 0.f);
+    const float4* src0 = one ? a.dr : a.dms;
+    for (int k = lane; k < PS; k += 32) {
+      const int l = k / NK, sl = k % NK;
+      Axis ay, ax;
+      if (!MX) {
+        Geo32 G;
+        G.init(a);
+        const float ct = cosf((float(l) + 0.5f) * dthetaf);
+        ay = make_axis(G.u_mu(a, r, ct, false), a.sc_mu);
+        ax = make_axis((float(sl - 1) + u_ms) / float(NNU), a.W);
+      } else {
+        ay = bounded_axis(a.g_iry[j * NT + l], a.sc_mu);
+        ax = bounded_axis(a.g_irx[i * NK + sl], a.W);
+      }
+      const float3 v = fetch3(src0, a.W, a.sc_mu, ax, ay, az);
+      P[k] = make_float4(v.x, v.y, v.z, 0.f);
+      if (one) {
+        const float3 m = fetch3(a.dm, a.W, a.sc_mu, ax, ay, az);
+        P[PS + k] = make_float4(m.x, m.y, m.z, 0.f);
+      }
     }
   }
   __syncthreads();
+  if (!active) return;
   const float sxs = sqrtf(1.0f - mu_s * mu_s);
   const float g = a.g;
   const float kmie = 3.0f / (8.0f * kPiF) * (1.0f - g * g) / (2.0f + g * g);
@@ -1383,62 +1419,49 @@ __device__ void tile_indirect(const DevAtmo& a, int order, int tile, unsigned ch
   const float fnu = float(NNU - 1);
   Kahan3 acc;
   acc.init();
-  for (int k = tid; k < NT * NP; k += nth) {
-    const int l = k / NP, m = k % NP;
-    const float theta = (float(l) + 0.5f) * dthetaf, phi = (float(m) + 0.5f) * dphif;
-    const float st = sinf(theta);
-    const float cx = cosf(phi) * st, ct = cosf(theta);
-    const float dom = dthetaf * dphif * st;
-    // nu = dot(omega, omega_s) with omega_s = (sqrt(1 - mu_s^2), 0, mu_s)
-    const float nu = cx * sxs + ct * mu_s;
-    const float tcx = (nu + 1.0f) / 2.0f * fnu;
-    float fk = floorf(tcx);
-    const float lf = tcx - fk;
-    fk = fminf(fmaxf(fk, -1.0f), float(NNU - 1));
-    const int ks = (int)fk + 1;
+  for (int l = 0; l < NT; ++l) {
+    const float2 row = Drow[l];
+    const float ct = row.x, dom = row.y;
     const float4* Pl = P + l * NK;
-    float3 L;
-    if (one) {
-      const float4* Ml = P + NT * NK + l * NK;
-      const float4 r0 = Pl[ks], r1 = Pl[ks + 1], m0 = Ml[ks], m1 = Ml[ks + 1];
-      const float pr = kray * (1.0f + nu * nu);
-      const float rs = rsqrtf(g1 - g2 * nu);
-      const float pm = kmie * (1.0f + nu * nu) * (rs * rs * rs);
-      L.x = fmaf(r1.x - r0.x, lf, r0.x) * pr + fmaf(m1.x - m0.x, lf, m0.x) * pm;
-      L.y = fmaf(r1.y - r0.y, lf, r0.y) * pr + fmaf(m1.y - m0.y, lf, m0.y) * pm;
-      L.z = fmaf(r1.z - r0.z, lf, r0.z) * pr + fmaf(m1.z - m0.z, lf, m0.z) * pm;
-    } else {
-      const float4 r0 = Pl[ks], r1 = Pl[ks + 1];
-      L.x = fmaf(r1.x - r0.x, lf, r0.x);
-      L.y = fmaf(r1.y - r0.y, lf, r0.y);
-      L.z = fmaf(r1.z - r0.z, lf, r0.z);
-    }
-    const float3 v = L * ct * dom;
-    if (!MX) {
-      acc.s.x += v.x;
-      acc.s.y += v.y;
-      acc.s.z += v.z;
-    } else {
-      acc.add(v);
+    for (int m = lane; m < NP; m += 32) {
+      // nu = dot(omega, omega_s) with omega_s = (sqrt(1 - mu_s^2), 0, mu_s)
+      const float nu = Dcx[l * NP + m] * sxs + ct * mu_s;
+      const float tcx = (nu + 1.0f) / 2.0f * fnu;
+      float fk = floorf(tcx);
+      const float lf = tcx - fk;
+      fk = fminf(fmaxf(fk, -1.0f), float(NNU - 1));
+      const int ks = (int)fk + 1;
+      float3 L;
+      if (one) {
+        const float4* Ml = Pl + PS;
+        const float4 r0 = Pl[ks], r1 = Pl[ks + 1], m0 = Ml[ks], m1 = Ml[ks + 1];
+        const float pr = kray * (1.0f + nu * nu);
+        const float rs = rsqrt_pos(g1 - g2 * nu);
+        const float pm = kmie * (1.0f + nu * nu) * (rs * rs * rs);
+        L.x = fmaf(r1.x - r0.x, lf, r0.x) * pr + fmaf(m1.x - m0.x, lf, m0.x) * pm;
+        L.y = fmaf(r1.y - r0.y, lf, r0.y) * pr + fmaf(m1.y - m0.y, lf, m0.y) * pm;
+        L.z = fmaf(r1.z - r0.z, lf, r0.z) * pr + fmaf(m1.z - m0.z, lf, m0.z) * pm;
+      } else {
+        const float4 r0 = Pl[ks], r1 = Pl[ks + 1];
+        L.x = fmaf(r1.x - r0.x, lf, r0.x);
+        L.y = fmaf(r1.y - r0.y, lf, r0.y);
+        L.z = fmaf(r1.z - r0.z, lf, r0.z);
+      }
+      const float3 v = L * ct * dom;
+      if (!MX) {
+        acc.s.x += v.x;
+        acc.s.y += v.y;
+        acc.s.z += v.z;
+      } else {
+        acc.add(v);
+      }
     }
   }
-  // reduction: warp shuffles, then the 8 warp sums in FP64 through shared memory
-  double sx = warp_sum((double)acc.s.x - (double)acc.c.x);
-  double sy = warp_sum((double)acc.s.y - (double)acc.c.y);
-  double sz = warp_sum((double)acc.s.z - (double)acc.c.z);
+  // reduction over the warp's lanes, in FP64
+  const double tx = warp_sum((double)acc.s.x - (double)acc.c.x);
+  const double ty = warp_sum((double)acc.s.y - (double)acc.c.y);
+  const double tz = warp_sum((double)acc.s.z - (double)acc.c.z);
   if (lane == 0) {
-    red[3 * warp] = sx;
-    red[3 * warp + 1] = sy;
-    red[3 * warp + 2] = sz;
-  }
-  __syncthreads();
-  if (tid == 0) {
-    double tx = 0, ty = 0, tz = 0;
-    for (int w = 0; w < nth / 32; ++w) {
-      tx += red[3 * w];
-      ty += red[3 * w + 1];
-      tz += red[3 * w + 2];
-    }
     const float3 res = make_float3((float)tx, (float)ty, (float)tz);
     a.dirr[(order + 1) & 1][t] = make_float4(res.x, res.y, res.z, 0.f);
     if (!MX) {
@@ -1821,7 +1844,6 @@ __host__ __device__ inline int tiles_rows(int W, int sc_mu, int sc_r) {
   return (sc_mu * sc_r + R - 1) / R;
 }
 __host__ __device__ inline int tiles_direct(int ir_mus, int ir_r) { return (ir_mus * ir_r + kThreads - 1) / kThreads; }
-__host__ __device__ inline int tiles_indirect(int ir_mus, int ir_r) { return ir_mus * ir_r; }
 __host__ __device__ inline int tiles_density(const DevAtmo& a) {
   return dens_shape(a.sc_r, a.sc_mu, a.sc_mus, a.sc_nu, a.dens_S, a.dens_chunk).tiles;
 }
