@@ -1603,22 +1603,33 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
   }
   // per-texel constants (TPT texels per thread): row, slab entry, texel x
   float c_rmus[TPT], c_nu[TPT], c_lerp[TPT];
-  int c_lr[TPT], c_e[TPT], c_x[TPT];
+  int c_lr[TPT], c_e[TPT], c_x[TPT], c_ro[TPT];
   // per-unit constants of the slab build (TPT units per thread; a unit is
   // four entries of one plane of a row, and a tile has at most as many units
-  // as texels since rows are at least 4 entries wide): row, float offset in
-  // the density row, slab offset, entries in use
+  // as texels since rows are at least 4 entries wide): row's record offset,
+  // float offset in the density row, slab offset, entries in use.
+  //
+  // The sample loop branches on warp-wide conditions only (warp votes), so
+  // that it needs no divergence handling: warps without units or texels skip
+  // that work, and in a warp with some, a lane without a unit repeats another
+  // lane's unit (the same values stored to the same entries) and a lane
+  // without a texel computes texel 0 of the tile and stores nothing.
   const int G4 = (W + 3) / 4, nunits = nrow * 3 * G4;
-  int u_lr[TPT], u_src[TPT], u_dst[TPT], u_n[TPT];
+  int u_ro[TPT], u_src[TPT], u_dst[TPT], u_n[TPT];
+  bool w_unit[TPT], w_tex[TPT], has_tex[TPT];
+  bool all_full = true;
 #pragma unroll
   for (int j = 0; j < TPT; ++j) {
-    const int u = tid + j * nth;
+    const int u0 = tid + j * nth, u = u0 < nunits ? u0 : u0 % nunits;
     const int lr = u / (3 * G4), rem = u - lr * 3 * G4, pl = rem / G4, g = rem - pl * G4;
-    u_lr[j] = lr;
+    u_ro[j] = lr * NS;
     u_src[j] = pl * a.Wd + 4 * g;
     u_dst[j] = (lr * 3 + pl) * SR + 4 * g;
     u_n[j] = min(4, W - 4 * g);
+    w_unit[j] = __any_sync(0xffffffffu, u0 < nunits);
+    all_full = all_full && u_n[j] == 4;
   }
+  all_full = __all_sync(0xffffffffu, all_full);
   Kahan3 acc[TPT];
   float3 part[TPT];
   MuS32 mus32;
@@ -1630,11 +1641,15 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
     acc[j].init();
     part[j] = make_float3(0.f, 0.f, 0.f);
     c_rmus[j] = c_nu[j] = c_lerp[j] = 0.f;
-    const int k = tid + j * nth;
+    const int k0 = tid + j * nth;
+    has_tex[j] = k0 < nx_tex;
+    w_tex[j] = __any_sync(0xffffffffu, has_tex[j]);
+    const int k = has_tex[j] ? k0 : 0;
     c_lr[j] = k / W;
     c_x[j] = k - c_lr[j] * W;
     c_e[j] = c_lr[j] * 3 * SR;
-    if (k < nx_tex) {
+    c_ro[j] = c_lr[j] * NS;
+    {
       float mu_s, nu, rmus;
       texel_mus_nu<MX>(a.g_rows[row0 + c_lr[j]], a.g_cols[c_x[j]], mu_s, nu, rmus);
       c_nu[j] = nu;
@@ -1660,8 +1675,8 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
   auto load = [&](int i) {
 #pragma unroll
     for (int j = 0; j < TPT; ++j) {
-      if (tid + j * nth < nunits) {
-        const MSRec& o = rec[u_lr[j] * NS + i];
+      if (w_unit[j]) {
+        const MSRec& o = rec[u_ro[j] + i];
         const float4* p = reinterpret_cast<const float4*>(dens + u_src[j]);
 #pragma unroll
         for (int c = 0; c < 4; ++c) q[j][c] = ld4(p + o.off[c]);
@@ -1671,8 +1686,8 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
   auto blend = [&](int i, float* dst) {
 #pragma unroll
     for (int j = 0; j < TPT; ++j) {
-      if (tid + j * nth < nunits) {
-        const MSRec& o = rec[u_lr[j] * NS + i];
+      if (w_unit[j]) {
+        const MSRec& o = rec[u_ro[j] + i];
         const float w00 = o.w[0], w10 = o.w[1], w01 = o.w[2], w11 = o.w[3];
         const float4 a00 = q[j][0], a10 = q[j][1], a01 = q[j][2], a11 = q[j][3];
         float4 v;
@@ -1681,7 +1696,7 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
         v.z = fmaf(w11, a11.z, fmaf(w01, a01.z, fmaf(w10, a10.z, w00 * a00.z)));
         v.w = fmaf(w11, a11.w, fmaf(w01, a01.w, fmaf(w10, a10.w, w00 * a00.w)));
         float* d = dst + u_dst[j];
-        if (u_n[j] == 4) {
+        if (all_full || u_n[j] == 4) {
           *reinterpret_cast<float4*>(d) = v;
         } else {
           d[0] = v.x;
@@ -1696,8 +1711,8 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
   auto step = [&](int i, const float* cur) {
 #pragma unroll
     for (int j = 0; j < TPT; ++j) {
-      if (tid + j * nth < nx_tex) {
-        const MSRec& o = rec[c_lr[j] * NS + i];
+      if (w_tex[j]) {
+        const MSRec& o = rec[c_ro[j] + i];
         const float nu = c_nu[j];
         // position within a nu slice, texel units (scattering.h:48-56, 149-151):
         // both slices of the lookup share it
@@ -1793,8 +1808,7 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
   // outputs: delta multiple scattering and the final table (:91-92)
 #pragma unroll
   for (int j = 0; j < TPT; ++j) {
-    const int k = tid + j * nth;
-    if (k < nx_tex) {
+    if (has_tex[j]) {
       const size_t t = (size_t)(row0 + c_lr[j]) * W + c_x[j];
       const float3 ms = make_float3(acc[j].s.x - acc[j].c.x, acc[j].s.y - acc[j].c.y, acc[j].s.z - acc[j].c.z);
       a.dms[t] = store_round4(make_float4(ms.x, ms.y, ms.z, 0.f), a.f16);
