@@ -1417,12 +1417,15 @@ __device__ void tile_indirect(const DevAtmo& a, int order, int tile, unsigned ch
   const float kray = 3.0f / (16.0f * kPiF);
   const float g1 = 1.0f + g * g, g2 = 2.0f * g;
   const float fnu = float(NNU - 1);
+  // each lane sums its directions of a theta row in FP32 (NP / 32 of them),
+  // then adds the row sum to a Kahan-compensated total
   Kahan3 acc;
   acc.init();
   for (int l = 0; l < NT; ++l) {
     const float2 row = Drow[l];
     const float ct = row.x, dom = row.y;
     const float4* Pl = P + l * NK;
+    float3 part = make_float3(0.f, 0.f, 0.f);
     for (int m = lane; m < NP; m += 32) {
       // nu = dot(omega, omega_s) with omega_s = (sqrt(1 - mu_s^2), 0, mu_s)
       const float nu = Dcx[l * NP + m] * sxs + ct * mu_s;
@@ -1448,13 +1451,16 @@ __device__ void tile_indirect(const DevAtmo& a, int order, int tile, unsigned ch
         L.z = fmaf(r1.z - r0.z, lf, r0.z);
       }
       const float3 v = L * ct * dom;
-      if (!MX) {
-        acc.s.x += v.x;
-        acc.s.y += v.y;
-        acc.s.z += v.z;
-      } else {
-        acc.add(v);
-      }
+      part.x += v.x;
+      part.y += v.y;
+      part.z += v.z;
+    }
+    if (!MX) {
+      acc.s.x += part.x;
+      acc.s.y += part.y;
+      acc.s.z += part.z;
+    } else {
+      acc.add(part);
     }
   }
   // reduction over the warp's lanes, in FP64
