@@ -337,20 +337,6 @@ def run_ours(a):
     torch.cuda.synchronize()
     e2e_s = max_over_ranks(world, time.perf_counter() - t0) / a.steps
     e2e = whole_job_rate(world, a.batch, e2e_s)
-    # one step's table copies alone (no build running beside them), for the
-    # record: the bandwidth the end-to-end figure has to hide behind kernels
-    p = build_batch(builder, params, stream=streams[0])
-    p.wait()
-    torch.cuda.synchronize()
-    c0 = time.perf_counter()
-    for i in range(a.batch):
-        base = hosts[0][i].ctypes.data
-        N.check(N.lib().fb_atmosphere_copy_to_host_async(p.atmosphere(i)._h, streams[0].cuda_stream, base,
-                                                         base + 4 * n_tr, base + 4 * (n_tr + n_ir)),
-                "fb_atmosphere_copy_to_host_async")
-    streams[0].synchronize()
-    copy_s = time.perf_counter() - c0
-    p.release()
 
     # plain path: one default-size atmosphere per call, FP32
     plain_p = Parameters()
@@ -425,8 +411,7 @@ def run_ours(a):
         "e2e": {"value": e2e, "unit": "atmospheres/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": a.batch * per_atm,
                 "overlap": "each step built as %d batches of %d on two streams: a batch's copies overlap the next "
-                           "batch's kernels" % (parts, sub),
-                "copies_alone_ms": copy_s * 1e3, "d2h_gbs_alone": a.batch * per_atm / copy_s / 1e9},
+                           "batch's kernels" % (parts, sub)},
         "gpu_launches": sum(len(x) for x in prof),
         "roofline": {"bound": "fp32", "kernel": "k_density (scattering density + indirect irradiance), order >= 3",
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s",

@@ -604,9 +604,9 @@ void plan_group(Plan& P, const std::vector<DevAtmo>& A, const std::vector<int>& 
     for (int j : jobs) {
       const DevAtmo& a = A[j];
       t0.push_back(fb::tiles_density(a));
-      t1.push_back(fb::tiles_indirect(a.ir_mus, a.ir_r, a.irr_n, a.sc_nu));
+      t1.push_back(fb::tiles_indirect(a.ir_mus, a.ir_r, a.irr_n, a.sc_nu, a.W, n - 1 == 1));
       D.smem = std::max(D.smem, fb::density_smem(a, n == 2, mixed, cl));
-      D.smem = std::max(D.smem, fb::indirect_smem(a.irr_n, a.sc_nu, n - 1 == 1));
+      D.smem = std::max(D.smem, fb::indirect_smem(a.irr_n, a.sc_nu, a.W, a.ir_mus, n - 1 == 1));
       D.texels += (uint64_t)a.W * a.sc_mu * a.sc_r + (uint64_t)a.ir_mus * a.ir_r;
     }
     add_segment(P, D, 0, jobs, t0);

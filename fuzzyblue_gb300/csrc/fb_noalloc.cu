@@ -245,8 +245,8 @@ extern "C" int fb_atmosphere_build_noalloc(void* stream, const fb_params* p, voi
   const int ms_block = fb::ms_threads(d.W);
   for (int n = 2; !rc && n <= d.order; ++n) {
     const bool cl = fb::density_smem(d, n == 2, mixed, false) > (size_t)std::max(0, ds->smem_optin - 1024);
-    const size_t sm = std::max(fb::density_smem(d, n == 2, mixed, cl), fb::indirect_smem(d.irr_n, d.sc_nu, n - 1 == 1));
-    rc = add(fb::kPassDensity, n, {fb::tiles_density(d), fb::tiles_indirect(d.ir_mus, d.ir_r, d.irr_n, d.sc_nu)}, sm, 1,
+    const size_t sm = std::max(fb::density_smem(d, n == 2, mixed, cl), fb::indirect_smem(d.irr_n, d.sc_nu, d.W, d.ir_mus, n - 1 == 1));
+    rc = add(fb::kPassDensity, n, {fb::tiles_density(d), fb::tiles_indirect(d.ir_mus, d.ir_r, d.irr_n, d.sc_nu, d.W, n - 1 == 1)}, sm, 1,
              fb::kDensThreads, cl ? fb::kDensClamped : 0);
     if (!rc)
       rc = add(fb::kPassMultiple, n, {fb::tiles_multiple(d.W, d.sc_mus, d.ms_steps, d.sc_mu, d.sc_r, ms_block)},

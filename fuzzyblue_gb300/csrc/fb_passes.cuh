@@ -10,7 +10,9 @@
 //                    multiple-scattering samples (seg 2)     thread per (row, sample)
 //                    density r / theta records (segment 3)   thread per record
 //   k_density        scattering_density.comp (segment 0)     CTA per (r, mu_s, mu-chunk)
-//                    indirect_irradiance.comp (segment 1)    CTA per texel
+//                    indirect_irradiance.comp (segment 1)    CTA per irradiance r row (up to 64 texels);
+//                                                            order 1: four texels, a warp each
+//                    scattering_density.comp (segment 1)     CTA per (r, mu_s, mu-chunk)
 //   k_multiple       multiple_scattering.comp                CTA per (mu, r) row(s)
 // CTAs take work items from a global atomic counter; an item is a tile of one
 // atmosphere, located by binary search over per-atmosphere item offsets.
@@ -792,6 +794,10 @@ __host__ __device__ inline DensShape dens_shape(int sc_r, int sc_mu, int sc_mus,
     d.S = max(1, min(sc_mus, kDensThreads / per_col));
     d.chunk = sc_mu;
   }
+  // the interval tables grow with S (nu + 2) records per theta row: with many
+  // nu slices, fewer columns per tile, so that the tables of up to 32 theta
+  // rows fit in shared memory
+  d.S = max(1, min(d.S, 4096 / (32 * (sc_nu + 2))));
   d.scols = (sc_mus + d.S - 1) / d.S;
   d.ychunks = (sc_mu + d.chunk - 1) / d.chunk;
   d.tiles = sc_r * d.scols * d.ychunks;
@@ -1336,10 +1342,38 @@ __host__ __device__ inline int ir_per_item(int irr_n, int sc_nu) {
   while (k > 1 && indirect_smem_k(irr_n, sc_nu, true, k) > kIrItemSmem) k >>= 1;
   return k;
 }
-__host__ __device__ inline size_t indirect_smem(int irr_n, int sc_nu, bool one) {
-  return indirect_smem_k(irr_n, sc_nu, one, ir_per_item(irr_n, sc_nu));
+// Row items (tile_indirect_rows): an item is up to KT irradiance texels of one
+// irradiance r row. Shared memory: the direction table, the table blended in
+// (mu, r) for one theta row over every x (B; order 1 blends the Rayleigh and
+// Mie tables through it in turn), the texels' slice entries of that theta row
+// (P, per table) and every thread's FP64 partial sums. KT is the largest of
+// 64, 32, 16 whose layout fits in kIrRowsSmem (the order-1 layout, the larger,
+// decides); 0 selects the per-texel items.
+__host__ __device__ inline size_t ir_rows_smem(int irr_n, int sc_nu, int W, bool one, int kt) {
+  const size_t NT = irr_n / 2, NP = 2 * (size_t)irr_n, f = one ? 2 : 1;
+  return align16(sizeof(float) * NT * NP) + align16(sizeof(float2) * NT) + align16(sizeof(float4) * W) +
+         align16(sizeof(float4) * (size_t)kt * (sc_nu + 2) * f) + sizeof(double) * 3 * kDensThreads;
 }
-__host__ __device__ inline int tiles_indirect(int ir_mus, int ir_r, int irr_n, int sc_nu) {
+constexpr size_t kIrRowsSmem = 48 * 1024;  // no more than the density tiles' own shared memory
+__host__ __device__ inline int ir_rows_kt(int irr_n, int sc_nu, int W, int ir_mus) {
+  for (int kt = 64; kt >= 16; kt >>= 1)
+    if (ir_rows_smem(irr_n, sc_nu, W, true, kt) <= kIrRowsSmem) return kt < ir_mus ? kt : ir_mus;
+  return 0;
+}
+// Row items integrate orders >= 2 (the multiple-scattering table); order 1
+// (the Rayleigh and Mie tables with their phase functions) keeps the items of
+// up to four texels, which measured faster there (173.3 against 175.3 ms per
+// order-2 density launch of 256 default atmospheres).
+__host__ __device__ inline int ir_items_kt(int irr_n, int sc_nu, int W, int ir_mus, bool one) {
+  return one ? 0 : ir_rows_kt(irr_n, sc_nu, W, ir_mus);
+}
+__host__ __device__ inline size_t indirect_smem(int irr_n, int sc_nu, int W, int ir_mus, bool one) {
+  const int kt = ir_items_kt(irr_n, sc_nu, W, ir_mus, one);
+  return kt ? ir_rows_smem(irr_n, sc_nu, W, one, kt) : indirect_smem_k(irr_n, sc_nu, one, ir_per_item(irr_n, sc_nu));
+}
+__host__ __device__ inline int tiles_indirect(int ir_mus, int ir_r, int irr_n, int sc_nu, int W, bool one) {
+  const int kt = ir_items_kt(irr_n, sc_nu, W, ir_mus, one);
+  if (kt) return ir_r * ((ir_mus + kt - 1) / kt);
   const int k = ir_per_item(irr_n, sc_nu);
   return (ir_mus * ir_r + k - 1) / k;
 }
@@ -1483,6 +1517,181 @@ __device__ void tile_indirect(const DevAtmo& a, int order, int tile, unsigned ch
   }
 }
 
+// Row items: KT irradiance texels of one irradiance r row. For each theta row
+// the CTA first blends the order's table in (mu, r) at that row's lookup
+// position for every x of the packed table (B; coalesced loads, each table
+// row read once for the item), then every texel's slice entries are linear
+// interpolations of B in x (P), then the texels' directions of that theta row
+// are summed. The interpolation is the same trilinear one (blended in y and
+// z, then in x). Each texel's directions are split over nth / KT threads
+// whose FP64 partial sums meet in shared memory.
+template <bool MX>
+__device__ void tile_indirect_rows(const DevAtmo& a, int order, int tile, int KT, unsigned char* smem) {
+  const int ord = order - 1;  // order integrated (the push constant order-1)
+  const bool one = ord == 1;
+  const int NT = a.irr_n / 2, NP = 2 * a.irr_n;
+  const int NNU = a.sc_nu, NK = NNU + 2, W = a.W;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  const int segs = (a.ir_mus + KT - 1) / KT;
+  const int j = tile / segs, i0 = (tile % segs) * KT;
+  const int nt = min(KT, a.ir_mus - i0);
+  float* Dcx = (float*)smem;                                          // NT * NP: cos phi sin theta
+  float2* Drow = (float2*)(smem + align16(sizeof(float) * NT * NP));  // NT: (cos theta, d omega)
+  float4* B = (float4*)((unsigned char*)Drow + align16(sizeof(float2) * NT));  // W
+  float4* P = (float4*)((unsigned char*)B + align16(sizeof(float4) * W));        // KT * NK (x2 for order 1)
+  double* X = (double*)((unsigned char*)P + align16(sizeof(float4) * (size_t)KT * NK * (one ? 2 : 1)));
+  const float dthetaf = kPiF / float(a.irr_n), dphif = kPiF / float(a.irr_n);
+  for (int k = tid; k < NT * NP; k += nth) {
+    const int l = k / NP, m = k % NP;
+    const float theta = (float(l) + 0.5f) * dthetaf, phi = (float(m) + 0.5f) * dphif;
+    Dcx[k] = cosf(phi) * sinf(theta);
+    if (m == 0) Drow[l] = make_float2(cosf(theta), dthetaf * dphif * sinf(theta));
+  }
+  // this irradiance row and the thread's texel (t) and share of its directions (h of H)
+  const int H = nth / KT, t = tid % KT, h = tid / KT;
+  const bool active = t < nt && h < H;
+  const int i = i0 + (t < nt ? t : 0);
+  float r = 0.f, mu_s, u_ms = 0.f;
+  Axis az;
+  if (!MX) {
+    Geo32 G;
+    G.init(a);
+    const float x_mu_s = float(i) / float(a.ir_mus - 1), x_r = float(j) / float(a.ir_r - 1);
+    r = G.R + x_r * (G.T - G.R);
+    mu_s = clamp_cosine(2.0f * x_mu_s - 1.0f);
+    az = make_axis(G.u_r(a, r), a.sc_r);
+    u_ms = G.u_mu_s(a, mu_s);
+  } else {
+    const IrZ z = a.g_irz[j];
+    r = z.r;
+    az = bounded_axis(z.az, a.sc_r);
+    mu_s = a.g_irmus[i];
+  }
+  const float4* src0 = one ? a.dr : a.dms;
+  const float sxs = sqrtf(1.0f - mu_s * mu_s);
+  const float g = a.g;
+  const float kmie = 3.0f / (8.0f * kPiF) * (1.0f - g * g) / (2.0f + g * g);
+  const float kray = 3.0f / (16.0f * kPiF);
+  const float g1 = 1.0f + g * g, g2 = 2.0f * g;
+  const float fnu = float(NNU - 1);
+  const int PS = KT * NK;
+  Kahan3 acc;
+  acc.init();
+  for (int l = 0; l < NT; ++l) {
+    // B: the table at this theta row's (mu, r) position, every x
+    Axis ay;
+    if (!MX) {
+      Geo32 G;
+      G.init(a);
+      ay = make_axis(G.u_mu(a, r, cosf((float(l) + 0.5f) * dthetaf), false), a.sc_mu);
+    } else {
+      ay = bounded_axis(a.g_iry[j * NT + l], a.sc_mu);
+    }
+    const float w00 = (1.0f - ay.f) * (1.0f - az.f), w10 = ay.f * (1.0f - az.f);
+    const float w01 = (1.0f - ay.f) * az.f, w11 = ay.f * az.f;
+    const size_t r00 = ((size_t)az.i0 * a.sc_mu + ay.i0) * W, r10 = ((size_t)az.i0 * a.sc_mu + ay.i1) * W;
+    const size_t r01 = ((size_t)az.i1 * a.sc_mu + ay.i0) * W, r11 = ((size_t)az.i1 * a.sc_mu + ay.i1) * W;
+    for (int tab = 0; tab < (one ? 2 : 1); ++tab) {
+      const float4* T = tab ? a.dm : src0;
+      for (int x = tid; x < W; x += nth) {
+        const float4 p00 = ld4(T + r00 + x), p10 = ld4(T + r10 + x), p01 = ld4(T + r01 + x), p11 = ld4(T + r11 + x);
+        B[x] = make_float4(fmaf(w11, p11.x, fmaf(w01, p01.x, fmaf(w10, p10.x, w00 * p00.x))),
+                           fmaf(w11, p11.y, fmaf(w01, p01.y, fmaf(w10, p10.y, w00 * p00.y))),
+                           fmaf(w11, p11.z, fmaf(w01, p01.z, fmaf(w10, p10.z, w00 * p00.z))), 0.f);
+      }
+      __syncthreads();
+      // P: each texel's entries of the nu slices -1 .. nu_size at its mu_s
+      float4* Pt = P + tab * PS;
+      for (int e = tid; e < nt * NK; e += nth) {
+        const int t2 = e / NK, sl = e - t2 * NK;
+        Axis ax;
+        if (!MX) {
+          Geo32 G;
+          G.init(a);
+          const float ms2 = clamp_cosine(2.0f * (float(i0 + t2) / float(a.ir_mus - 1)) - 1.0f);
+          ax = make_axis((float(sl - 1) + G.u_mu_s(a, ms2)) / float(NNU), a.W);
+        } else {
+          ax = bounded_axis(a.g_irx[(i0 + t2) * NK + sl], a.W);
+        }
+        const float4 b0 = B[ax.i0], b1 = B[ax.i1];
+        const float f0 = 1.0f - ax.f;
+        Pt[e] = make_float4(fmaf(ax.f, b1.x, f0 * b0.x), fmaf(ax.f, b1.y, f0 * b0.y), fmaf(ax.f, b1.z, f0 * b0.z), 0.f);
+      }
+      __syncthreads();
+    }
+    if (active) {
+      const float2 row = Drow[l];
+      const float ct = row.x, dom = row.y;
+      const float4* Pl = P + t * NK;
+      float3 part = make_float3(0.f, 0.f, 0.f);
+      for (int m = h; m < NP; m += H) {
+        // nu = dot(omega, omega_s) with omega_s = (sqrt(1 - mu_s^2), 0, mu_s)
+        const float nu = Dcx[l * NP + m] * sxs + ct * mu_s;
+        const float tcx = (nu + 1.0f) / 2.0f * fnu;
+        float fk = floorf(tcx);
+        const float lf = tcx - fk;
+        fk = fminf(fmaxf(fk, -1.0f), float(NNU - 1));
+        const int ks = (int)fk + 1;
+        float3 L;
+        if (one) {
+          const float4* Ml = Pl + PS;
+          const float4 r0 = Pl[ks], r1 = Pl[ks + 1], m0 = Ml[ks], m1 = Ml[ks + 1];
+          const float pr = kray * (1.0f + nu * nu);
+          const float rs = rsqrt_pos(g1 - g2 * nu);
+          const float pm = kmie * (1.0f + nu * nu) * (rs * rs * rs);
+          L.x = fmaf(r1.x - r0.x, lf, r0.x) * pr + fmaf(m1.x - m0.x, lf, m0.x) * pm;
+          L.y = fmaf(r1.y - r0.y, lf, r0.y) * pr + fmaf(m1.y - m0.y, lf, m0.y) * pm;
+          L.z = fmaf(r1.z - r0.z, lf, r0.z) * pr + fmaf(m1.z - m0.z, lf, m0.z) * pm;
+        } else {
+          const float4 r0 = Pl[ks], r1 = Pl[ks + 1];
+          L.x = fmaf(r1.x - r0.x, lf, r0.x);
+          L.y = fmaf(r1.y - r0.y, lf, r0.y);
+          L.z = fmaf(r1.z - r0.z, lf, r0.z);
+        }
+        const float3 v = L * ct * dom;
+        part.x += v.x;
+        part.y += v.y;
+        part.z += v.z;
+      }
+      if (!MX) {
+        acc.s.x += part.x;
+        acc.s.y += part.y;
+        acc.s.z += part.z;
+      } else {
+        acc.add(part);
+      }
+    }
+    __syncthreads();  // B and P are rebuilt for the next theta row
+  }
+  // the texel's partial sums, in FP64
+  X[3 * tid] = (double)acc.s.x - (double)acc.c.x;
+  X[3 * tid + 1] = (double)acc.s.y - (double)acc.c.y;
+  X[3 * tid + 2] = (double)acc.s.z - (double)acc.c.z;
+  __syncthreads();
+  if (h == 0 && t < nt) {
+    double tx = 0.0, ty = 0.0, tz = 0.0;
+    for (int q = 0; q < H; ++q) {
+      const int o = 3 * (q * KT + t);
+      tx += X[o];
+      ty += X[o + 1];
+      tz += X[o + 2];
+    }
+    const int tt = j * a.ir_mus + i;
+    const float3 res = make_float3((float)tx, (float)ty, (float)tz);
+    a.dirr[(order + 1) & 1][tt] = make_float4(res.x, res.y, res.z, 0.f);
+    if (!MX) {
+      const float4 old = a.ir[tt];
+      a.ir[tt] = make_float4(res.x + old.x, res.y + old.y, res.z + old.z, 0.f + old.w);
+    } else {
+      double* acc3 = a.ir_acc + 3 * (size_t)tt;
+      acc3[0] += tx;
+      acc3[1] += ty;
+      acc3[2] += tz;
+      a.ir[tt] = make_float4((float)acc3[0], (float)acc3[1], (float)acc3[2], 0.f);
+    }
+  }
+}
+
 // V selects the occupancy variant chosen by the autotuner: V = 0 caps the
 // registers for 4 resident blocks per SM, V = 1 for 3, V = 2 for 5. TWO: the
 // launch of order 2, whose lookups read the single-scattering Rayleigh and
@@ -1493,8 +1702,18 @@ __global__ void __launch_bounds__(kDensThreads, V == 0 ? 4 : (V == 1 ? 3 : 5)) k
   int seg, job, tile;
   int taken = 0;
   while (next_item(L, seg, job, tile, taken)) {
-    if (seg == 0) tile_density<MX, TWO, CL>(L.atm[job], L.order, tile, smem);
-    else tile_indirect<MX>(L.atm[job], L.order, tile, smem);
+    if (seg == 0) {
+      tile_density<MX, TWO, CL>(L.atm[job], L.order, tile, smem);
+    } else {
+      const DevAtmo& a = L.atm[job];
+      // order 2 (TWO) integrates order 1, which always takes the four-texel
+      // items: its kernel does not contain the row items
+      const int kt = TWO ? 0 : ir_items_kt(a.irr_n, a.sc_nu, a.W, a.ir_mus, false);
+      if (!TWO && kt)
+        tile_indirect_rows<MX>(a, L.order, tile, kt, smem);
+      else
+        tile_indirect<MX>(a, L.order, tile, smem);
+    }
   }
 }
 

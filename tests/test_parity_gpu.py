@@ -279,3 +279,16 @@ def test_batch_with_clamped_tables_equals_single_builds(builder):
         ref = gpu_build(builder, p)
         for k in ("transmittance", "irradiance", "scattering"):
             assert np.array_equal(o[k], ref[k]), k
+
+
+def test_indirect_per_texel_items_match_fp64(builder, oracle):
+    """Sizes whose indirect-irradiance row items would not fit in shared
+    memory (64 nu slices, rows of 2048 texels, 64 irradiance samples: 32 x 128
+    directions) fall back to items of one irradiance texel; MIXED meets the
+    FP64 target there too."""
+    p = smoke_parameters(order=3, precision=PRECISION_MIXED).replace(
+        scattering_nu_size=64, scattering_mu_s_size=32, scattering_r_size=2, scattering_mu_size=4,
+        irradiance_samples=64, irradiance_mu_s_size=16, irradiance_r_size=4)
+    out = gpu_build(builder, p)
+    ref = oracle.precompute(p, dtype=np.float64)
+    _check(out, ref, ("transmittance", "irradiance", "scattering"), MIXED_MAX)
