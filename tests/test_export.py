@@ -71,3 +71,44 @@ def test_export_atmosphere(builder, tmp_path):
         assert np.array_equal(np.load(npy[name]), tables[name])
     assert np.array_equal(np.load(npy["scattering_f16"]), half)
     pend.release()
+
+
+def test_exr_bytes_match_the_file_format(tmp_path):
+    """A two-channel 2 x 2 file assembled byte by byte from the published
+    OpenEXR layout (magic number, version field, attributes as name, type
+    name, size and value, header terminator, one 64-bit offset per scanline,
+    then per scanline its y, its byte count and each channel's row with the
+    channels in name order), independent of `write_exr` and `read_exr`."""
+    a = np.array([[1.0, 2.0], [3.0, 4.0]], np.float32)          # FLOAT
+    b = np.array([[0.5, -2.0], [65504.0, 0.0]], np.float16)     # HALF
+    path = str(tmp_path / "k.exr")
+    export.write_exr(path, {"B": b, "A": a})  # given out of name order
+    got = open(path, "rb").read()
+
+    def attr(name, typ, value_hex):
+        v = bytes.fromhex(value_hex)
+        return name + b"\0" + typ + b"\0" + len(v).to_bytes(4, "little") + v
+
+    chlist = ("41 00" "02000000" "00 000000" "01000000" "01000000"     # "A", FLOAT, pLinear 0, sampling 1 1
+              "42 00" "01000000" "00 000000" "01000000" "01000000"     # "B", HALF
+              "00")
+    header = b"".join([
+        bytes.fromhex("762f3101"),          # magic 20000630
+        bytes.fromhex("02000000"),          # version 2, single-part scanline, no flags
+        attr(b"channels", b"chlist", chlist),
+        attr(b"compression", b"compression", "00"),                     # NO_COMPRESSION
+        attr(b"dataWindow", b"box2i", "00000000" "00000000" "01000000" "01000000"),
+        attr(b"displayWindow", b"box2i", "00000000" "00000000" "01000000" "01000000"),
+        attr(b"lineOrder", b"lineOrder", "00"),                         # INCREASING_Y
+        attr(b"pixelAspectRatio", b"float", "0000803f"),                # 1.0
+        attr(b"screenWindowCenter", b"v2f", "00000000" "00000000"),
+        attr(b"screenWindowWidth", b"float", "0000803f"),
+        b"\0",
+    ])
+    row = 2 * 4 + 2 * 2                      # A: two floats, B: two halves
+    first = len(header) + 2 * 8              # after the offset table
+    expect = header + (first).to_bytes(8, "little") + (first + 8 + row).to_bytes(8, "little")
+    # scanline 0: A = 1.0 2.0, B = 0.5 -2.0; scanline 1: A = 3.0 4.0, B = 65504 0
+    expect += bytes.fromhex("00000000" "0c000000" "0000803f" "00000040" "0038" "00c0")
+    expect += bytes.fromhex("01000000" "0c000000" "00004040" "00008040" "ff7b" "0000")
+    assert got == expect
