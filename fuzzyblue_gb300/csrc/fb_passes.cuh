@@ -952,7 +952,9 @@ struct DensRowConst {
   float inv_h, c1;           // TWO: nu = w inv_h + c1
   int nP, nE;                 // records per nu table row and of the ground irradiance table
 };
-template <bool TWO, bool GROUND, bool CL>
+// GC: the texels per thread when known at compile time (kDensMaxGroup, the
+// classes with nu a multiple of 8), else 0 and G at run time.
+template <bool TWO, bool GROUND, bool CL, int GC>
 __device__ __forceinline__ void dens_row(const DensLayout& S, const DensTheta& t, int l, int NT,
                                          const LerpRec* __restrict__ Pl,
                                          const DensRowConst& q, const float (&sx)[kDensMaxGroup],
@@ -973,7 +975,7 @@ __device__ __forceinline__ void dens_row(const DensLayout& S, const DensTheta& t
     const float3 cf = pc.eval(nu2, t.domega);
 #pragma unroll
     for (int j = 0; j < kDensMaxGroup; ++j) {
-      if (j < G) {
+      if (j < (GC ? GC : G)) {
         const float base = fmaf(sx[j], d.x, mus_ct), dy = sy[j] * d.y;
 #pragma unroll
         for (int side = 0; side < 2; ++side) {
@@ -1285,10 +1287,17 @@ __device__ void tile_density(const DevAtmo& a, int order, int tile, unsigned cha
       const size_t row = (size_t)(cl * NT + l) * MK;
       const LerpRec* Pl = TWO ? reinterpret_cast<const LerpRec*>(reinterpret_cast<const LerpRec2*>(S.P) + row)
                               : S.P + row;
-      if (t.ground)
-        dens_row<TWO, true, CL>(S, t, l, NT, Pl, q, sx, sy, G, pc, acc);
-      else
-        dens_row<TWO, false, CL>(S, t, l, NT, Pl, q, sx, sy, G, pc, acc);
+      if (G == kDensMaxGroup) {
+        if (t.ground)
+          dens_row<TWO, true, CL, kDensMaxGroup>(S, t, l, NT, Pl, q, sx, sy, G, pc, acc);
+        else
+          dens_row<TWO, false, CL, kDensMaxGroup>(S, t, l, NT, Pl, q, sx, sy, G, pc, acc);
+      } else {
+        if (t.ground)
+          dens_row<TWO, true, CL, 0>(S, t, l, NT, Pl, q, sx, sy, G, pc, acc);
+        else
+          dens_row<TWO, false, CL, 0>(S, t, l, NT, Pl, q, sx, sy, G, pc, acc);
+      }
       if (MX && ((l + 1) % kDensKahanRows == 0 || l == NT - 1)) {
         // Kahan sum over theta rows of the FP32 sums over kDensKahanRows rows
 #pragma unroll
@@ -1786,6 +1795,11 @@ __device__ __forceinline__ int row_pos(float t, float n_minus_1, float& f) {
   return max(__float_as_int(y) - kRoundMagicBits, 0);
 }
 
+// Compile-time switch of the multiple-scattering sample loop's lambdas.
+template <bool B> struct MsFast {
+  static constexpr bool value = B;
+};
+
 template <bool MX, int TPT>
 __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned char* smem) {
   const int W = a.W, nrows = a.sc_mu * a.sc_r, NM = a.sc_mus;
@@ -1897,10 +1911,12 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
   // use, leaving the zero guard alone.
   constexpr bool kAhead = TPT == 1;
   float4 q[TPT][4];
-  auto load = [&](int i) {
+  // `fast` (MsFast<true>): the warp has a unit and a texel in every slot and
+  // every unit is full, so the per-slot tests fold away
+  auto load = [&](auto fast, int i) {
 #pragma unroll
     for (int j = 0; j < TPT; ++j) {
-      if (w_unit[j]) {
+      if (decltype(fast)::value || w_unit[j]) {
         const MSRec& o = rec[u_ro[j] + i];
         const float4* p = reinterpret_cast<const float4*>(dens + u_src[j]);
 #pragma unroll
@@ -1908,10 +1924,10 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
       }
     }
   };
-  auto blend = [&](int i, float* dst) {
+  auto blend = [&](auto fast, int i, float* dst) {
 #pragma unroll
     for (int j = 0; j < TPT; ++j) {
-      if (w_unit[j]) {
+      if (decltype(fast)::value || w_unit[j]) {
         const MSRec& o = rec[u_ro[j] + i];
         const float w00 = o.w[0], w10 = o.w[1], w01 = o.w[2], w11 = o.w[3];
         const float4 a00 = q[j][0], a10 = q[j][1], a01 = q[j][2], a11 = q[j][3];
@@ -1921,7 +1937,7 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
         v.z = fmaf(w11, a11.z, fmaf(w01, a01.z, fmaf(w10, a10.z, w00 * a00.z)));
         v.w = fmaf(w11, a11.w, fmaf(w01, a01.w, fmaf(w10, a10.w, w00 * a00.w)));
         float* d = dst + u_dst[j];
-        if (all_full || u_n[j] == 4) {
+        if (decltype(fast)::value || all_full || u_n[j] == 4) {
           *reinterpret_cast<float4*>(d) = v;
         } else {
           d[0] = v.x;
@@ -1932,11 +1948,12 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
     }
   };
   const float fmus = float(NM);
-  // the texel work of sample i on its slab
-  auto step = [&](int i, const float* cur) {
+  // the texel work of sample i on its slab; `close`: sample i ends a run of
+  // the mixed sums (i % 8 == 7 or the last sample)
+  auto step = [&](auto fast, int i, const float* cur, bool close) {
 #pragma unroll
     for (int j = 0; j < TPT; ++j) {
-      if (w_tex[j]) {
+      if (decltype(fast)::value || w_tex[j]) {
         const MSRec& o = rec[c_ro[j] + i];
         const float nu = c_nu[j];
         // position within a nu slice, texel units (scattering.h:48-56, 149-151):
@@ -1965,7 +1982,7 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
         } else {
           // plain sums over runs of 8 samples, Kahan-compensated across runs
           part[j] = fma3(J, tvw, part[j]);
-          if ((i & 7) == 7 || i == N) {
+          if (close) {
             acc[j].add(part[j]);
             part[j] = make_float3(0.f, 0.f, 0.f);
           }
@@ -1982,29 +1999,60 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
   float* const sb3 = slab + 3 * slab_stride;
   static_assert(kMsSlabs == 4, "four slab buffers");
   // sample k from `cur` while sample k + A is built into `nxt`
+  const MsFast<false> slow;
+  const MsFast<true> quick;
   auto visit = [&](int k, const float* cur, float* nxt, int A) {
     if (k < NS) {
-      if (kAhead && k + A < NS) load(k + A);
-      step(k, cur);
+      if (kAhead && k + A < NS) load(slow, k + A);
+      step(slow, k, cur, (k & 7) == 7 || k == N);
       if (k + A < NS) {
-        if (!kAhead) load(k + A);
-        blend(k + A, nxt);
+        if (!kAhead) load(slow, k + A);
+        blend(slow, k + A, nxt);
       }
     }
   };
+  // the same where samples k and k + A exist; sample k ends a run if `close`
+  auto visit_full = [&](auto fast, int k, const float* cur, float* nxt, int A, bool close) {
+    if (kAhead) load(fast, k + A);
+    step(fast, k, cur, close);
+    if (!kAhead) load(fast, k + A);
+    blend(fast, k + A, nxt);
+  };
+  const bool fast = TPT == 1 && all_full && w_unit[0] && w_tex[0];  // warp-uniform
+  int i = 0;
   if (MX) {
     // two samples per barrier: i and i + 1 from their slabs while i + 2 and
     // i + 3 are built (measured faster for the mixed kernels; the plain ones
-    // run faster one sample per barrier)
-    load(0);
-    blend(0, sb0);
+    // run faster one sample per barrier). The loops first take the samples
+    // whose successors two ahead exist, without bounds tests.
+    load(slow, 0);
+    blend(slow, 0, sb0);
     if (NS > 1) {
-      load(1);
-      blend(1, sb1);
+      load(slow, 1);
+      blend(slow, 1, sb1);
     }
     __syncthreads();
     if (TPT == 1) {
-      for (int i = 0; i < NS; i += 4) {
+      for (; i + 5 < NS; i += 4) {
+        const bool c = (i & 4) != 0;  // sample i + 3 ends a run of 8
+        if (fast) {
+          visit_full(quick, i, sb0, sb2, 2, false);
+          visit_full(quick, i + 1, sb1, sb3, 2, false);
+        } else {
+          visit_full(slow, i, sb0, sb2, 2, false);
+          visit_full(slow, i + 1, sb1, sb3, 2, false);
+        }
+        __syncthreads();
+        if (fast) {
+          visit_full(quick, i + 2, sb2, sb0, 2, false);
+          visit_full(quick, i + 3, sb3, sb1, 2, c);
+        } else {
+          visit_full(slow, i + 2, sb2, sb0, 2, false);
+          visit_full(slow, i + 3, sb3, sb1, 2, c);
+        }
+        __syncthreads();
+      }
+      for (; i < NS; i += 4) {
         visit(i, sb0, sb2, 2);
         visit(i + 1, sb1, sb3, 2);
         __syncthreads();
@@ -2013,7 +2061,18 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
         __syncthreads();
       }
     } else {
-      for (int i = 0; i < NS; i += 2) {
+      for (; i + 3 < NS; i += 2) {
+        float* const b0 = slab + (i % kMsSlabs) * slab_stride;
+        float* const b1 = slab + ((i + 1) % kMsSlabs) * slab_stride;
+        float* const b2 = slab + ((i + 2) % kMsSlabs) * slab_stride;
+        float* const b3 = slab + ((i + 3) % kMsSlabs) * slab_stride;
+        // (a second copy for `fast` warps spills at this width)
+        const bool c = (i & 7) == 6;  // sample i + 1 ends a run of 8
+        visit_full(slow, i, b0, b2, 2, false);
+        visit_full(slow, i + 1, b1, b3, 2, c);
+        __syncthreads();
+      }
+      for (; i < NS; i += 2) {
         visit(i, slab + (i % kMsSlabs) * slab_stride, slab + ((i + 2) % kMsSlabs) * slab_stride, 2);
         visit(i + 1, slab + ((i + 1) % kMsSlabs) * slab_stride, slab + ((i + 3) % kMsSlabs) * slab_stride, 2);
         __syncthreads();
@@ -2022,10 +2081,10 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
   } else {
     // one sample per barrier: i from its slab while i + 1 is built (a
     // four-sample body with fixed buffers measured slower here)
-    load(0);
-    blend(0, sb0);
+    load(slow, 0);
+    blend(slow, 0, sb0);
     __syncthreads();
-    for (int i = 0; i < NS; ++i) {
+    for (; i < NS; ++i) {
       visit(i, slab + (i % kMsSlabs) * slab_stride, slab + ((i + 1) % kMsSlabs) * slab_stride, 1);
       __syncthreads();
     }
