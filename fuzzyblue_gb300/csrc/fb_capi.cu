@@ -628,6 +628,9 @@ void plan_group(Plan& P, const std::vector<DevAtmo>& A, const std::vector<int>& 
     M.nseg = 1;
     M.variant = fb::ms_block_variant(M.block) >= 0 ? fb::ms_block_variant(M.block)
                                                    : launch_variant(A, jobs, tun, mixed, false);
+    bool fixed = M.block == fb::kThreads && M.tpt == 1;
+    for (int j : jobs) fixed = fixed && fb::ms_fixed_layout(A[j].W, A[j].sc_mus);
+    if (fixed) M.variant += 4;  // 0, 1 -> 4, 5
     P.launches.push_back(M);
   }
 }

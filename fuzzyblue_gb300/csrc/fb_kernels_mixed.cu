@@ -12,6 +12,8 @@ template __global__ void k_multiple<true, 1, 2>(LaunchArgs);
 template __global__ void k_multiple<true, 2, 2>(LaunchArgs);
 template __global__ void k_multiple<true, 1, 3>(LaunchArgs);
 template __global__ void k_multiple<true, 2, 3>(LaunchArgs);
+template __global__ void k_multiple<true, 1, 4>(LaunchArgs);
+template __global__ void k_multiple<true, 1, 5>(LaunchArgs);
 
 template __global__ void k_density<true, 0, false, false>(LaunchArgs);
 template __global__ void k_density<true, 1, false, false>(LaunchArgs);
@@ -48,7 +50,9 @@ const void* kernel_mixed(int pass, int tpt, int variant, bool order2) {
     case kPassMultiple:
       if (variant == 2) return tpt >= 2 ? (const void*)k_multiple<true, 2, 2> : (const void*)k_multiple<true, 1, 2>;
       if (variant == 3) return tpt >= 2 ? (const void*)k_multiple<true, 2, 3> : (const void*)k_multiple<true, 1, 3>;
-      return v1 ? (const void*)k_multiple<true, 1, 1> : (const void*)k_multiple<true, 1, 0>;
+      if (variant == 4 && tpt == 1) return (const void*)k_multiple<true, 1, 4>;
+      if (variant == 5 && tpt == 1) return (const void*)k_multiple<true, 1, 5>;
+      return v1 || variant == 5 ? (const void*)k_multiple<true, 1, 1> : (const void*)k_multiple<true, 1, 0>;
   }
   return nullptr;
 }

@@ -243,6 +243,9 @@ extern "C" int fb_atmosphere_build_noalloc(void* stream, const fb_params* p, voi
               multi ? fb::tiles_msrec(d.sc_mu, d.sc_r, d.ms_steps) : 0, multi ? fb::tiles_densgeo(d.sc_r, d.dens_n) : 0},
              fb::ss_smem(d.W, d.ss_steps, d.sc_mus, d.sc_nu), 1, fb::kThreads, 0);
   const int ms_block = fb::ms_threads(d.W);
+  const int ms_tpt = fb::ms_shape(d.W, d.sc_mus, d.ms_steps, ms_block).TPT;
+  const int ms_variant = fb::ms_block_variant(ms_block) >= 0 ? fb::ms_block_variant(ms_block)
+                         : (ms_tpt == 1 && fb::ms_fixed_layout(d.W, d.sc_mus) ? 4 : 0);
   for (int n = 2; !rc && n <= d.order; ++n) {
     const bool cl = fb::density_smem(d, n == 2, mixed, false) > (size_t)std::max(0, ds->smem_optin - 1024);
     const size_t sm = std::max(fb::density_smem(d, n == 2, mixed, cl), fb::indirect_smem(d.irr_n, d.sc_nu, d.W, d.ir_mus, n - 1 == 1));
@@ -250,8 +253,7 @@ extern "C" int fb_atmosphere_build_noalloc(void* stream, const fb_params* p, voi
              fb::kDensThreads, cl ? fb::kDensClamped : 0);
     if (!rc)
       rc = add(fb::kPassMultiple, n, {fb::tiles_multiple(d.W, d.sc_mus, d.ms_steps, d.sc_mu, d.sc_r, ms_block)},
-               fb::ms_smem(d.W, d.ms_steps, d.sc_mus, ms_block), fb::ms_shape(d.W, d.sc_mus, d.ms_steps, ms_block).TPT,
-               ms_block, std::max(0, fb::ms_block_variant(ms_block)));
+               fb::ms_smem(d.W, d.ms_steps, d.sc_mus, ms_block), ms_tpt, ms_block, ms_variant);
   }
   if (rc) return rc;
 

@@ -1751,6 +1751,10 @@ constexpr int kMsMidThreads = 512;
 // are built.
 constexpr int kMsSlabs = 4;
 constexpr int kMsWideThreads = 1024;
+// The default table layout (32 mu_s texels, 8 nu slices), for which the
+// multiple-scattering kernels are also compiled with the sizes fixed (the
+// slab offsets of the texel loads become constants).
+constexpr int kMsFixedMuS = 32, kMsFixedW = 8 * kMsFixedMuS;
 constexpr int kMsRowBytes = 96 * 1024;  // shared memory for the rows of a tile (records + slabs)
 struct MSShape {
   int R;         // rows per tile
@@ -1773,6 +1777,11 @@ __host__ __device__ inline int ms_threads(int W) {
 // sizes, -1 for kThreads (the tuned occupancy variant 0 or 1 applies).
 __host__ __device__ inline int ms_block_variant(int block) {
   return block == kMsWideThreads ? 2 : (block == kMsMidThreads ? 3 : -1);
+}
+// An atmosphere of the fixed layout: with CTAs of kThreads (one texel per
+// thread) its launches may take variants 4 and 5.
+__host__ __device__ inline bool ms_fixed_layout(int W, int sc_mus) {
+  return W == kMsFixedW && sc_mus == kMsFixedMuS;
 }
 __host__ __device__ inline int tiles_multiple(int W, int sc_mus, int steps, int sc_mu, int sc_r, int threads) {
   const MSShape m = ms_shape(W, sc_mus, steps, threads);
@@ -1800,10 +1809,12 @@ template <bool B> struct MsFast {
   static constexpr bool value = B;
 };
 
-template <bool MX, int TPT>
+// NMC, WC: the mu_s size and row width when fixed at compile time (the slab
+// offsets of the texel loads become constants), else 0; NTH: the CTA size.
+template <bool MX, int TPT, int NMC, int WC, int NTH>
 __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned char* smem) {
-  const int W = a.W, nrows = a.sc_mu * a.sc_r, NM = a.sc_mus;
-  const int nth = blockDim.x;
+  const int W = WC ? WC : a.W, nrows = a.sc_mu * a.sc_r, NM = NMC ? NMC : a.sc_mus;
+  const int nth = NTH;
   const MSShape sh = ms_shape(W, NM, a.ms_steps, nth);
   const int row0 = tile * sh.R;
   const int nrow = min(sh.R, nrows - row0);
@@ -2121,15 +2132,24 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
 
 // V = 0: CTAs of kThreads, registers capped for 4 resident CTAs per SM;
 // V = 1: for 3; V = 2: CTAs of kMsWideThreads, one per SM; V = 3: CTAs of
-// kMsMidThreads, two per SM.
+// kMsMidThreads, two per SM; V = 4, 5: as 0, 1 for launches whose atmospheres
+// all have the fixed layout (ms_fixed_layout), compiled with its sizes.
 template <bool MX, int TPT, int V>
 __global__ void __launch_bounds__(V == 2 ? kMsWideThreads : (V == 3 ? kMsMidThreads : kThreads),
-                                  V == 2 ? 1 : (V == 3 ? 2 : (V == 0 ? 4 : 3)))
+                                  V == 2 ? 1 : (V == 3 ? 2 : (V == 0 || V == 4 ? 4 : 3)))
     k_multiple(LaunchArgs L) {
   extern __shared__ __align__(16) unsigned char smem[];
   int seg, job, tile;
   int taken = 0;
-  while (next_item(L, seg, job, tile, taken)) tile_multiple<MX, TPT>(L.atm[job], L.order, tile, smem);
+  constexpr int NTH = V == 2 ? kMsWideThreads : (V == 3 ? kMsMidThreads : kThreads);
+  constexpr bool FIX = V >= 4;
+  static_assert(!FIX || TPT == 1, "the fixed layout has one texel per thread");
+  if (blockDim.x != NTH) return;  // the launch plans give each variant its CTA size
+  while (next_item(L, seg, job, tile, taken)) {
+    const DevAtmo& a = L.atm[job];
+    if (FIX && !ms_fixed_layout(a.W, a.sc_mus)) continue;  // the launch plans never pair these
+    tile_multiple<MX, TPT, FIX ? kMsFixedMuS : 0, FIX ? kMsFixedW : 0, NTH>(a, L.order, tile, smem);
+  }
 }
 
 // ------------------------------------------------------ tile geometry ----
