@@ -669,8 +669,14 @@ __device__ void tile_single(const DevAtmo& a, int tile, unsigned char* smem) {
   __syncthreads();
   const float TT = a.top * a.top;
   const float trc0 = 0.5f / float(a.tr_mu), trc1 = 1.0f - 1.0f / float(a.tr_mu), trn = float(a.tr_mu);
+  // Texels go to threads nu slice fastest: a warp holds a few neighbouring
+  // mu_s columns of every nu slice, whose sun directions at a sample (and so
+  // transmittance lookups) lie closer together than those of a warp along
+  // mu_s, so its lookups touch fewer cache sectors.
+  const int NU = a.sc_nu, NMS = a.sc_mus;
   for (int k = tid; k < nrow * W; k += kThreads) {
-    const int lr = k / W, x = k % W;
+    const int lr = k / W, kx = k - lr * W, kn = kx / NU;
+    const int x = (kx - kn * NU) * NMS + kn;  // nu slice kx % NU, mu_s column kx / NU
     const RowGeo& ri = rows[lr];
     float mu_s, nu, r_mu_s;
     texel_mus_nu<MX>(ri, a.g_cols[x], mu_s, nu, r_mu_s);
