@@ -104,47 +104,21 @@ __device__ __forceinline__ double warp_sum(double v) {
 
 // ===================================================================== T ===
 // transmittance.comp:8-80. One warp per texel; lanes split the trapezoid
-// samples of the three optical lengths, then reduce with shuffles.
+// samples of the three optical lengths, then reduce with shuffles. A work
+// item is kTrPerWarp texels per warp, so that the barriers with which a CTA
+// takes an item are spread over more texels.
+constexpr int kTrPerWarp = 4;
+constexpr int kTrTexels = kThreads / 32 * kTrPerWarp;  // texels per work item
 template <bool MX> __device__ void tile_transmittance(const DevAtmo& a, int tile) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int t0 = tile * (kThreads / 32);
-  const int t = t0 + warp;
+  const int t0 = tile * kTrTexels;
   const int ntr = a.tr_mu * a.tr_r;
   const int N = a.tr_steps;
-  float sR, sM, sA;
-  if (!MX) {
-    if (t >= ntr) return;
-    const int i = t % a.tr_mu, j = t / a.tr_mu;
-    Geo32 G;
-    G.init(a);
-    float x_mu = float(i) / float(a.tr_mu - 1), x_r = float(j) / float(a.tr_r - 1);
-    // transmittance.comp:48-64
-    float rho = G.H * x_r;
-    float r = sqrtf(rho * rho + G.R * G.R);
-    float d_min = G.T - r, d_max = rho + G.H;
-    float d = d_min + x_mu * (d_max - d_min);
-    float mu = d == 0.0f ? 1.0f : (G.H * G.H - rho * rho - d * d) / (2.0f * r * d);
-    mu = clamp_cosine(mu);
-    const float dx = G.dist_top(r, mu) / float(N);
-    const float two_r_mu = 2.0f * r * mu, rr = r * r;
-    sR = sM = sA = 0.0f;
-    for (int k = lane; k <= N; k += 32) {
-      float d_i = float(k) * dx;
-      float r_i = sqrtf(d_i * d_i + two_r_mu * d_i + rr);
-      float h = r_i - G.R;
-      float w = (k == 0 || k == N) ? 0.5f : 1.0f;
-      sR += profile_density(a.ray_d, h) * w * dx;
-      sM += profile_density(a.mie_d, h) * w * dx;
-      sA += profile_density(a.abs_d, h) * w * dx;
-    }
-    sR = warp_sum(sR);
-    sM = warp_sum(sM);
-    sA = warp_sum(sA);
-  } else {
-    // The ray state of the CTA's texels (transmittance.comp:48-64 in FP64)
-    // is computed once per texel by one thread and shared: (q, 2 s, dx).
-    __shared__ float3 s_ray[kThreads / 32];
-    if (threadIdx.x < kThreads / 32 && t0 + (int)threadIdx.x < ntr) {
+  // MIXED: the ray state of the item's texels (transmittance.comp:48-64 in
+  // FP64) is computed once per texel by one thread and shared: (q, 2 s, dx).
+  __shared__ float3 s_ray[kTrTexels];
+  if (MX) {
+    if (threadIdx.x < kTrTexels && t0 + (int)threadIdx.x < ntr) {
       const int tt = t0 + threadIdx.x;
       const int i = tt % a.tr_mu, j = tt / a.tr_mu;
       Geo64 G;
@@ -157,55 +131,89 @@ template <bool MX> __device__ void tile_transmittance(const DevAtmo& a, int tile
       s_ray[threadIdx.x] = make_float3((float)q, (float)(2.0 * s), (float)(G.dist_top(q, s) / double(N)));
     }
     __syncthreads();
-    if (t >= ntr) return;
-    // The march runs in FP32 on the FP64 ray state: r_k^2 - R^2 =
-    // q + d_k (2 s + d_k) keeps the altitude q_k / (r_k + R) free of the
-    // cancellation of r_k - R, to ~1e-5 km where the ray grazes the ground.
-    const float3 ray = s_ray[warp];
-    const float qf = ray.x, two_sf = ray.y, dxf = ray.z, Rf = a.bottom, R2f = Rf * Rf;
-    float cR = 0.f, cM = 0.f, cA = 0.f;
-    sR = sM = sA = 0.0f;
-    for (int k = lane; k <= N; k += 32) {
-      const float d_k = float(k) * dxf;
-      const float q_k = fmaf(d_k, two_sf + d_k, qf);
-      const float r_k = sqrtf(q_k + R2f);
-      // every ray of this table stays at or above the ground: a negative
-      // altitude here is rounding at a tangent sample
-      float h = gmax(__fdividef(q_k, r_k + Rf), 0.0f);
-      float w = (k == 0 || k == N) ? 0.5f : 1.0f;
-      Kahan3::add1(sR, cR, profile_density(a.ray_d, h) * w);
-      Kahan3::add1(sM, cM, profile_density(a.mie_d, h) * w);
-      Kahan3::add1(sA, cA, profile_density(a.abs_d, h) * w);
-    }
-    // compensated lane sums, reduced in FP32 (32 terms)
-    sR = warp_sum(sR - cR) * dxf;
-    sM = warp_sum(sM - cM) * dxf;
-    sA = warp_sum(sA - cA) * dxf;
   }
-  if (lane == 0) {
-    float4 o;
-    o.x = expf(-(a.rayleigh[0] * sR + a.mie_ext[0] * sM + a.absorption[0] * sA));
-    o.y = expf(-(a.rayleigh[1] * sR + a.mie_ext[1] * sM + a.absorption[1] * sA));
-    o.z = expf(-(a.rayleigh[2] * sR + a.mie_ext[2] * sM + a.absorption[2] * sA));
-    o.w = 1.0f;
-    a.tr[t] = o;
-    // the pair table: this texel's RGB first in its own record, second in the
-    // record of texel i - 1 and, at the last mu, in its own
-    const int i = t % a.tr_mu;
-    float* own = a.trp + 8 * (size_t)t;
-    own[0] = o.x;
-    own[1] = o.y;
-    own[2] = o.z;
-    own[6] = own[7] = 0.f;
-    if (i > 0) {
-      own[-5] = o.x;
-      own[-4] = o.y;
-      own[-3] = o.z;
+  for (int m = 0; m < kTrPerWarp; ++m) {
+    const int tl = m * (kThreads / 32) + warp;  // texel of the item
+    const int t = t0 + tl;
+    if (t >= ntr) break;
+    float sR, sM, sA;
+    if (!MX) {
+      const int i = t % a.tr_mu, j = t / a.tr_mu;
+      Geo32 G;
+      G.init(a);
+      float x_mu = float(i) / float(a.tr_mu - 1), x_r = float(j) / float(a.tr_r - 1);
+      // transmittance.comp:48-64
+      float rho = G.H * x_r;
+      float r = sqrtf(rho * rho + G.R * G.R);
+      float d_min = G.T - r, d_max = rho + G.H;
+      float d = d_min + x_mu * (d_max - d_min);
+      float mu = d == 0.0f ? 1.0f : (G.H * G.H - rho * rho - d * d) / (2.0f * r * d);
+      mu = clamp_cosine(mu);
+      const float dx = G.dist_top(r, mu) / float(N);
+      const float two_r_mu = 2.0f * r * mu, rr = r * r;
+      sR = sM = sA = 0.0f;
+      for (int k = lane; k <= N; k += 32) {
+        float d_i = float(k) * dx;
+        float r_i = sqrtf(d_i * d_i + two_r_mu * d_i + rr);
+        float h = r_i - G.R;
+        float w = (k == 0 || k == N) ? 0.5f : 1.0f;
+        sR += profile_density(a.ray_d, h) * w * dx;
+        sM += profile_density(a.mie_d, h) * w * dx;
+        sA += profile_density(a.abs_d, h) * w * dx;
+      }
+      sR = warp_sum(sR);
+      sM = warp_sum(sM);
+      sA = warp_sum(sA);
+    } else {
+      // The march runs in FP32 on the FP64 ray state: r_k^2 - R^2 =
+      // q + d_k (2 s + d_k) keeps the altitude q_k / (r_k + R) free of the
+      // cancellation of r_k - R, to ~1e-5 km where the ray grazes the ground.
+      const float3 ray = s_ray[tl];
+      const float qf = ray.x, two_sf = ray.y, dxf = ray.z, Rf = a.bottom, R2f = Rf * Rf;
+      float cR = 0.f, cM = 0.f, cA = 0.f;
+      sR = sM = sA = 0.0f;
+      for (int k = lane; k <= N; k += 32) {
+        const float d_k = float(k) * dxf;
+        const float q_k = fmaf(d_k, two_sf + d_k, qf);
+        const float r_k = sqrtf(q_k + R2f);
+        // every ray of this table stays at or above the ground: a negative
+        // altitude here is rounding at a tangent sample
+        float h = gmax(__fdividef(q_k, r_k + Rf), 0.0f);
+        float w = (k == 0 || k == N) ? 0.5f : 1.0f;
+        Kahan3::add1(sR, cR, profile_density(a.ray_d, h) * w);
+        Kahan3::add1(sM, cM, profile_density(a.mie_d, h) * w);
+        Kahan3::add1(sA, cA, profile_density(a.abs_d, h) * w);
+      }
+      // compensated lane sums, reduced in FP32 (32 terms)
+      sR = warp_sum(sR - cR) * dxf;
+      sM = warp_sum(sM - cM) * dxf;
+      sA = warp_sum(sA - cA) * dxf;
     }
-    if (i == a.tr_mu - 1) {
-      own[3] = o.x;
-      own[4] = o.y;
-      own[5] = o.z;
+    if (lane == 0) {
+      float4 o;
+      o.x = expf(-(a.rayleigh[0] * sR + a.mie_ext[0] * sM + a.absorption[0] * sA));
+      o.y = expf(-(a.rayleigh[1] * sR + a.mie_ext[1] * sM + a.absorption[1] * sA));
+      o.z = expf(-(a.rayleigh[2] * sR + a.mie_ext[2] * sM + a.absorption[2] * sA));
+      o.w = 1.0f;
+      a.tr[t] = o;
+      // the pair table: this texel's RGB first in its own record, second in the
+      // record of texel i - 1 and, at the last mu, in its own
+      const int i = t % a.tr_mu;
+      float* own = a.trp + 8 * (size_t)t;
+      own[0] = o.x;
+      own[1] = o.y;
+      own[2] = o.z;
+      own[6] = own[7] = 0.f;
+      if (i > 0) {
+        own[-5] = o.x;
+        own[-4] = o.y;
+        own[-3] = o.z;
+      }
+      if (i == a.tr_mu - 1) {
+        own[3] = o.x;
+        own[4] = o.y;
+        own[5] = o.z;
+      }
     }
   }
 }
@@ -2161,7 +2169,7 @@ __global__ void __launch_bounds__(V == 2 ? kMsWideThreads : (V == 3 ? kMsMidThre
 // ------------------------------------------------------ tile geometry ----
 // Host and device agree on tile counts and shared-memory sizes through these.
 __host__ __device__ inline int tiles_transmittance(int tr_mu, int tr_r) {
-  return (tr_mu * tr_r + kThreads / 32 - 1) / (kThreads / 32);
+  return (tr_mu * tr_r + kTrTexels - 1) / kTrTexels;
 }
 __host__ __device__ inline int tiles_rows(int W, int sc_mu, int sc_r) {
   const int R = rows_per_tile(W);
