@@ -298,7 +298,9 @@ typedef struct fb_tile_shape {
     uint32_t density_rows;     /* mu rows per scattering-density tile */
     uint32_t density_variant;  /* density kernel: 0, 1, 2 = registers for 4, 3, 5 blocks per SM;
                                   3-5: the same with exact-size interval tables */
-    uint32_t multiple_variant; /* occupancy variant of the multiple-scattering kernel */
+    uint32_t multiple_variant; /* multiple-scattering kernel: 0, 1 = registers for 4, 3 blocks
+                                  per SM (rows of the default layout, 32 mu_s x 8 nu, run
+                                  the same variant compiled for that layout) */
     float density_ms;          /* measured time of the chosen density launch */
     float multiple_ms;         /* measured time of the chosen multiple-scattering launch */
 } fb_tile_shape;
