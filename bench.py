@@ -175,7 +175,7 @@ FLOP_PER_ATMOSPHERE = 350185724984.0  # default sizes, 4 orders (same count)
 # is reported with "stale": true.
 KERNEL_SOURCES = ("fuzzyblue_gb300/csrc/fb_passes.cuh", "fuzzyblue_gb300/csrc/fb_device.cuh")
 DENSITY_NCU = {
-    "sources": "d14108b567563556",
+    "sources": "90e9a1b8a1402918",
     "profile": "profiles/passes_uniform16_mixed_ncu.md",
     "atmospheres": 16,
     "fp32_flop_per_direction_order3": 24.49,
@@ -185,11 +185,16 @@ DENSITY_NCU = {
 
 
 def kernel_sources_sha():
+    """SHA-256 prefix of the kernel sources' code: comments, trailing blanks and
+    empty lines removed, so that an edit of a comment keeps the counts current."""
     import hashlib
+    import re
     h = hashlib.sha256()
     for f in KERNEL_SOURCES:
-        with open(os.path.join(ROOT, f), "rb") as fh:
-            h.update(fh.read())
+        with open(os.path.join(ROOT, f), encoding="utf-8") as fh:
+            text = re.sub(r"/\*.*?\*/", "", fh.read(), flags=re.S)
+        lines = (re.sub(r"//.*", "", line).rstrip() for line in text.splitlines())
+        h.update("\n".join(line for line in lines if line).encode())
     return h.hexdigest()[:16]
 
 

@@ -3,17 +3,18 @@
 // with --fmad=false) and fb_kernels_mixed.cu (MX = true).
 //
 // Launch structure (one launch per pass group, any number of atmospheres):
-//   k_transmittance  transmittance.comp                      warp per texel
+//   k_transmittance  transmittance.comp                      warp per texel, four per work item
 //                    geometry tables: rows, x columns (seg 1) thread per entry
-//   k_single         single_scattering.comp  (segment 0)     CTA per (mu, r) row(s)
+//   k_single         single_scattering.comp  (segment 0)     CTA per (mu, r) row(s), texels
+//                                                            to threads nu slice fastest
 //                    direct_irradiance.comp  (segment 1)     thread per texel
 //                    multiple-scattering samples (seg 2)     thread per (row, sample)
 //                    density r / theta records (segment 3)   thread per record
 //   k_density        scattering_density.comp (segment 0)     CTA per (r, mu_s, mu-chunk)
 //                    indirect_irradiance.comp (segment 1)    CTA per irradiance r row (up to 64 texels);
 //                                                            order 1: four texels, a warp each
-//                    scattering_density.comp (segment 1)     CTA per (r, mu_s, mu-chunk)
-//   k_multiple       multiple_scattering.comp                CTA per (mu, r) row(s)
+//   k_multiple       multiple_scattering.comp                CTA per (mu, r) row(s); variants 4
+//                                                            and 5 compiled for the default layout
 // CTAs take work items from a global atomic counter; an item is a tile of one
 // atmosphere, located by binary search over per-atmosphere item offsets.
 #pragma once
