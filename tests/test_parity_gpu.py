@@ -215,6 +215,23 @@ def test_batch_of_mixed_widths_equals_single_builds(builder):
 
 
 @pytest.mark.parametrize("precision", [0, PRECISION_MIXED])
+def test_default_layout_variant_equals_generic_kernel(builder, precision):
+    """Rows of the default layout (32 mu_s texels by 8 nu slices) run the
+    multiple-scattering kernel compiled for that layout in a launch of their
+    own and the generic kernel in a launch shared with another size: the same
+    bits either way."""
+    from fuzzyblue_gb300.api import build_batch
+    d = Parameters(order=3, precision=precision)
+    pend = build_batch(builder, [d, smoke_parameters(order=3, precision=precision)])
+    pend.wait()
+    shared = pend.atmosphere(0).to_host()
+    pend.release()
+    alone = gpu_build(builder, d)
+    for k in ("transmittance", "irradiance", "scattering"):
+        assert np.array_equal(shared[k], alone[k]), k
+
+
+@pytest.mark.parametrize("precision", [0, PRECISION_MIXED])
 def test_odd_sizes_match_oracle(builder, oracle, precision):
     """Sizes the reference's dispatch would leave partly uncomputed (not
     multiples of its workgroup sizes, src/precompute.rs:1742,1797), odd mu_s
