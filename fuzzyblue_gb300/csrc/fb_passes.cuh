@@ -1939,11 +1939,22 @@ __device__ void tile_multiple(const DevAtmo& a, int order, int tile, unsigned ch
   float4 q[TPT][4];
   // `fast` (MsFast<true>): the warp has a unit and a texel in every slot and
   // every unit is full, so the per-slot tests fold away
+  // Samples are loaded in order. With one row per tile (the fixed layout) all
+  // threads load the same four density rows, and a sample in the same (mu, r)
+  // cell as the one before (the offsets of two opposite corners fix all four)
+  // keeps the values already loaded.
+  int prev0 = -1, prev3 = -1;
   auto load = [&](auto fast, int i) {
 #pragma unroll
     for (int j = 0; j < TPT; ++j) {
       if (decltype(fast)::value || w_unit[j]) {
         const MSRec& o = rec[u_ro[j] + i];
+        if (NMC) {
+          const int o0 = o.off[0], o3 = o.off[3];
+          if (o0 == prev0 && o3 == prev3) continue;
+          prev0 = o0;
+          prev3 = o3;
+        }
         const float4* p = reinterpret_cast<const float4*>(dens + u_src[j]);
 #pragma unroll
         for (int c = 0; c < 4; ++c) q[j][c] = ld4(p + o.off[c]);
