@@ -175,12 +175,12 @@ FLOP_PER_ATMOSPHERE = 350185724984.0  # default sizes, 4 orders (same count)
 # is reported with "stale": true.
 KERNEL_SOURCES = ("fuzzyblue_gb300/csrc/fb_passes.cuh", "fuzzyblue_gb300/csrc/fb_device.cuh")
 DENSITY_NCU = {
-    "sources": "90e9a1b8a1402918",
+    "sources": "3c8e1ac1b66b0be0",
     "profile": "profiles/passes_uniform16_mixed_ncu.md",
     "atmospheres": 16,
     "fp32_flop_per_direction_order3": 24.49,
     "thread_instr_per_direction_order3": 20.54,
-    "dram_bytes_per_atmosphere_order3": 13.23e6,
+    "dram_bytes_per_atmosphere_order3": 13.16e6,
 }
 
 
