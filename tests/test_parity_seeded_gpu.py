@@ -9,7 +9,8 @@
    test_parity_gpu.test_each_pass_at_default_size, plus the rows of rays at the
    horizon, where the transmittance table changes by large factors per texel);
    at the sizes of the crate's dump example (r16 mu64 mu_s16 nu4, 4 orders) the
-   whole precompute against the FP64 oracle on every texel.
+   whole precompute against the FP64 oracle on every texel, and in PLAIN
+   precision against the FP64 oracle, bounded by the FP32 oracle's own error.
 2. Orders 5-8 (the uneven and serving workloads draw orders in 2-8; the
    reference's order loop, src/precompute.rs:1853-1999, accumulates every
    order into the scattering and irradiance tables,
@@ -32,7 +33,7 @@ import pytest
 
 from fuzzyblue_gb300 import workloads
 from fuzzyblue_gb300.params import PRECISION_MIXED, Parameters, dump_parameters, smoke_parameters
-from tests.errors import summary
+from tests.errors import rel_err, summary
 
 pytestmark = pytest.mark.gpu
 
@@ -143,6 +144,35 @@ def test_headline_draw_end_to_end_dump_size(builder, oracle, i):
     ref = oracle.precompute(p, np.float64)
     for k in KEYS:
         _check64("headline draw %d, dump size, order 4" % i, k, out[k], ref[k])
+
+
+@pytest.mark.parametrize("i", [0, 6, 95, 161, 216])
+def test_headline_draw_plain_dump_size(builder, oracle, i):
+    """The draws in PLAIN precision (the reference's FP32 arithmetic), whole
+    precompute at the dump size. In these thin atmospheres the reference's
+    FP32 arithmetic is itself ill-conditioned in places (the FP32 oracle is
+    up to 67 % off FP64 in irradiance for draw 216, 52 % in scattering for
+    draw 0), where two FP32 evaluations that round differently disagree. So,
+    texel by texel, PLAIN must be no farther from the FP64 oracle than
+    max(2e-3, 2 x the FP32 oracle's own distance from FP64), as the per-pass
+    check of test_parity_gpu does for the default atmosphere."""
+    q = dump_parameters()
+    p = _draws()[i].replace(scattering_r_size=q.scattering_r_size, scattering_mu_size=q.scattering_mu_size,
+                            scattering_mu_s_size=q.scattering_mu_s_size, scattering_nu_size=q.scattering_nu_size,
+                            precision=0)
+    out = _build(builder, p)
+    r32 = oracle.precompute(p)
+    r64 = oracle.precompute(p, np.float64)
+    for k in KEYS:
+        got = np.asarray(out[k])
+        assert np.isfinite(got).all(), k
+        _report("headline draw %d, dump size, order 4, plain vs FP32" % i, k, summary(got, r32[k]))
+        e_gpu = rel_err(got, r64[k]).max(axis=-1)
+        e_ref = rel_err(np.asarray(r32[k], np.float64), r64[k]).max(axis=-1)
+        print("PARITY headline draw %d, plain | %s | gpu vs FP64 max %.3e, FP32 oracle vs FP64 max %.3e"
+              % (i, k, e_gpu.max(), e_ref.max()))
+        bad = np.flatnonzero(e_gpu > np.maximum(PLAIN_MAX, 2.0 * e_ref))
+        assert bad.size == 0, (k, bad[:8], e_gpu.reshape(-1)[bad[:8]], e_ref.reshape(-1)[bad[:8]])
 
 
 @pytest.mark.parametrize("size", ["smoke", "dump"])
